@@ -1,0 +1,198 @@
+/*
+ * pm_gb300.h -- C ABI of the GB300-native PatchMatch-Stereo densifier for
+ * equirectangular keyframes.
+ *
+ * It sits where RoblabWh/PatchMatch's densification thread calls into its
+ * CUDA file: a reference keyframe plus its neighbour keyframes go in; depth,
+ * normal, plane, score and best-view maps, a geometric-consistency-filtered
+ * depth map and a fused, coloured point cloud come out.  All signatures use
+ * plain pointers and sizes.  Every function returns a status code (PM_OK = 0)
+ * and records a message retrievable with pm_last_error(); nothing is printed.
+ * The reference's launchers return void and only print cudaGetLastError
+ * (src/openvslam/PatchMatchCuda.cu:447-451).
+ *
+ * Conventions (as in the reference):
+ *   - images are H x W row-major; pixel (i, j) = (row, column);
+ *   - pixel (i, j) has bearing (cos lat sin lon, -sin lat, cos lat cos lon),
+ *     lon = 2 pi (j/W - 1/2), lat = -pi (i/H - 1/2)  (PatchMatchCuda.cu:183-208);
+ *   - poses are world->camera: X_c = R_cw X_w + t_cw, R_cw row-major;
+ *   - a plane hypothesis is the camera-frame vector pi with pi . X = 1, so the
+ *     depth (range) of pixel (i, j) is 1 / |pi . b(i, j)|  (PatchMatchCuda.cu:31-43,402-404).
+ *
+ * Thread safety: one context may be used from one host thread at a time; use
+ * one context per thread for concurrency.  No process-global state is kept
+ * (the reference kept poses in __constant__ symbols, PatchMatchCuda.cu:11-23).
+ */
+#ifndef PM_GB300_H
+#define PM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PM_MAX_SOURCES 10
+
+/* status codes */
+#define PM_OK 0
+#define PM_EINVAL 1      /* bad argument (size, pointer, pose, parameter) */
+#define PM_ENOMEM 2      /* device allocation failed */
+#define PM_EBUDGET 3     /* request does not fit the context's HBM budget */
+#define PM_ETIMEOUT 4    /* a bounded wait expired */
+#define PM_ECUDA 5       /* CUDA runtime error (message in pm_last_error) */
+#define PM_ENOTREADY 6   /* asynchronous work still in flight */
+#define PM_ECANCELLED 7  /* request was cancelled */
+#define PM_ENOTBUILT 8   /* no kernel variant for this configuration */
+
+/* view combination (how per-source NCC scores become one cost) */
+#define PM_COMBINE_FOLD 0  /* reference GPU rule: running "average if within 25 %, else max" (PatchMatchCuda.cu:161-171) */
+#define PM_COMBINE_MAX 1   /* reference CPU rule: maximum over sources (depthmap.cc:1104-1127) */
+#define PM_COMBINE_TOPK 2  /* per-pixel view selection: mean of the top_k sources */
+
+/* longitude seam handling of bilinear source samples */
+#define PM_SEAM_CLAMP 0    /* clamp at the image border (the reference's texture behaviour) */
+#define PM_SEAM_WRAP 1     /* wrap around in longitude (360-degree continuity) */
+
+/* initialisation */
+#define PM_INIT_LOGUNIFORM_HEMI 0 /* log-uniform depth, unit normals on the camera-facing hemisphere */
+#define PM_INIT_REF_UNIFORM 1     /* uniform depth, normal components U[-1,1] (PatchMatchCuda.cu:210-244) */
+
+/* image storage */
+#define PM_IMAGE_U8 0
+#define PM_IMAGE_F16 1
+
+typedef struct {
+    int patch_half;      /* taps at odd offsets -patch_half..patch_half (5 = PatchSize 7 - 2, depthmap.cc:725) */
+    int iterations;      /* red-black sweeps (Dense.Iterations, config.cc:172) */
+    int combine;         /* PM_COMBINE_* */
+    int top_k;           /* sources averaged by PM_COMBINE_TOPK */
+    int seam;            /* PM_SEAM_* */
+    int init_mode;       /* PM_INIT_* */
+    int image_format;    /* PM_IMAGE_* of pm_view.gray */
+    int postprocess;     /* 1: host-equivalent window, median and thresholds (depthmap.cc:731-767) */
+    float min_depth;     /* initialisation range and accepted depth range */
+    float max_depth;
+    float min_score;     /* 0.1 (depthmap_computation_module.cc:223) */
+    float min_patch_sd;  /* low-texture mask threshold (Dense.MinPatchSD, 0 disables) */
+    float sigma_color;   /* bilateral sigmas 50 and 5 (PatchMatchCuda.cu:897-900) */
+    float sigma_x;
+    uint32_t seed;       /* Philox key, with keyframe_id */
+    uint32_t keyframe_id;
+} pm_params;
+
+typedef struct {
+    const void *gray;     /* H x W intensities, uint8 or IEEE half per pm_params.image_format */
+    size_t pitch_bytes;   /* row pitch; 0 = tightly packed */
+    const uint8_t *mask;  /* optional H x W (reference view only): 0 = pixel ignored */
+    double R_cw[9];       /* world->camera rotation, row-major */
+    double t_cw[3];
+} pm_view;
+
+typedef struct {
+    float *depth;         /* H x W, 0 = invalid (required) */
+    float *score;         /* H x W or NULL */
+    float *plane;         /* H x W x 3 or NULL */
+    float *normal;        /* H x W x 3 or NULL: unit, camera frame, facing the camera */
+    int32_t *best_view;   /* H x W or NULL: 0-based index of the best source */
+} pm_maps;
+
+typedef struct pm_ctx pm_ctx;
+typedef struct pm_request pm_request;
+
+/* Defaults of the reference path: patch_half 5, iterations 8, fold
+ * combination, clamp seam, log-uniform/hemisphere init in [0.3, 20] m,
+ * u8 images, post-processing on, min_score 0.1, sigmas 50/5. */
+void pm_params_default(pm_params *p);
+
+/* Context: one CUDA stream on `device`, device buffers owned by the context,
+ * an HBM budget for admission (0 = 90 % of free memory).
+ * Replaces the per-keyframe cudaMalloc/cudaFree of
+ * DepthmapEstimator::ComputePatchMatch (depthmap.cc:557-800) and the global
+ * constant-memory state of InitConstantMem (PatchMatchCuda.cu:885-912). */
+int pm_create(int device, size_t hbm_budget_bytes, pm_ctx **out);
+int pm_destroy(pm_ctx *ctx);
+const char *pm_last_error(const pm_ctx *ctx);
+const char *pm_status_string(int status);
+/* Kernel launches issued by this context so far (instrumentation). */
+uint64_t pm_launch_count(const pm_ctx *ctx);
+
+/* One keyframe, host buffers in and out (synchronous).  views[0] is the
+ * reference keyframe, views[1..n_views-1] its sources (1..PM_MAX_SOURCES).
+ * Replaces DepthmapEstimator::ComputePatchMatch (depthmap.cc:541-806):
+ * bearing table, random initialisation, init scoring, red-black sweeps,
+ * host post-filter. */
+int pm_densify(pm_ctx *ctx, int width, int height, const pm_view *views, int n_views, const pm_params *params,
+               pm_maps *out);
+
+/* ---- device-resident requests (the building block of batching/serving) ---- */
+/* Allocate device state for one W x H keyframe with n_sources sources.
+ * Fails with PM_EBUDGET when the context's HBM budget would be exceeded. */
+int pm_request_create(pm_ctx *ctx, int width, int height, int n_sources, const pm_params *params,
+                      pm_request **out);
+int pm_request_destroy(pm_request *req);
+size_t pm_request_bytes(int width, int height, int n_sources, int image_format);
+int pm_request_set_params(pm_request *req, const pm_params *params);
+/* Upload view k (0 = reference, 1.. = sources) asynchronously and build its
+ * sampling form.  Replaces InitTextureImages + InitConstantMem
+ * (PatchMatchCuda.cu:697-797,885-912). */
+int pm_request_set_view(pm_request *req, int k, const pm_view *view);
+/* Random planes (Philox) + scoring of every interior pixel.  Replaces
+ * ComputeRandomSeed + RandomInitialization (PatchMatchCuda.cu:621-663). */
+int pm_request_init(pm_request *req);
+/* Overwrite the plane map (H x W x 3, camera frame) and rescore it: the
+ * seeding entry for prior knowledge (replaces the host round trip of
+ * depthmap.cc:669-719). scores may be NULL (then every interior pixel is rescored). */
+int pm_request_set_state(pm_request *req, const float *planes, const float *scores);
+/* n_half red/black half-sweeps starting at half-sweep index first_half
+ * (even = red, odd = black; sweep = first_half / 2).  Replaces
+ * PatchMatchRedBlackPass (PatchMatchCuda.cu:568-615). */
+int pm_request_sweep(pm_request *req, int first_half, int n_half);
+/* Host-equivalent post-filter on the device (depthmap.cc:731-767,1169-1208). */
+int pm_request_postprocess(pm_request *req);
+/* init + all sweeps + post-filter, replayed from a captured CUDA graph. */
+int pm_request_run(pm_request *req);
+/* Copy maps to the host (synchronous). raw = 1 returns the unfiltered sweep state. */
+int pm_request_read(pm_request *req, pm_maps *out, int raw);
+int pm_request_synchronize(pm_request *req);
+/* Device pointer of the (filtered) depth map, H x W float, for chaining
+ * into pm_filter/pm_fuse without a host round trip. */
+const float *pm_request_depth_device(const pm_request *req);
+
+/* Score n fixed plane hypotheses at pixels ij[2n] (row, col) against the
+ * request's views: the cost kernel in isolation.  scores[n], best[n] and
+ * per_source[n * n_sources] may be NULL.  Replaces ScorePlaneDepth
+ * (PatchMatchCuda.cu:255-270,528-565) for arbitrary hypotheses. */
+int pm_score_hypotheses(pm_request *req, int n, const int32_t *ij, const float *planes, float *scores,
+                        int32_t *best, float *per_source);
+
+/* Geometric-consistency filter of depths[center] against the other views
+ * (host buffers).  A pixel is kept when at least min_consistent_views views
+ * (itself included) see the reprojected depth within same_depth_threshold
+ * relative; reproj_px > 0 adds a round-trip reprojection test of that many
+ * pixels.  Replaces DepthmapCleaner::Clean (depthmap.cc:1320-1377). */
+int pm_filter_consistency(pm_ctx *ctx, int width, int height, int n_views, const float *const *depths,
+                          const double *R_cw, const double *t_cw, int center, float same_depth_threshold,
+                          int min_consistent_views, float reproj_px, float *out);
+
+typedef struct {
+    int capacity;      /* entries available in the arrays below */
+    int count;         /* points written */
+    double *xyz;       /* capacity x 3 world coordinates (FP64, composed on the host) */
+    uint8_t *bgr;      /* capacity x 3 colour of the head keyframe (BGR) or NULL */
+    int32_t *ij;       /* capacity x 2 pixel (row, col) or NULL */
+} pm_points;
+
+/* Point fusion of the head map depths[0] against depths[1..n_views-1]:
+ * duplicate points are resolved in favour of the nearer observation and the
+ * later maps are edited in place (pixels zeroed), exactly in the order the
+ * reference does it.  pruned (H x W) receives the head's kept depth.
+ * Replaces DepthmapPruner::Prune (depthmap.cc:1535-1696). */
+int pm_fuse(pm_ctx *ctx, int width, int height, int n_views, float *const *depths, const double *R_cw,
+            const double *t_cw, const uint8_t *bgr, float same_depth_threshold, float *pruned, pm_points *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

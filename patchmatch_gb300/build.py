@@ -1,0 +1,98 @@
+"""In-tree build of the native libraries (no CMake, no setuptools).
+
+    python -m patchmatch_gb300.build
+
+Compiles the CUDA densifier for sm_103a into ``_lib/libpm_gb300.so`` (one
+translation unit per source-count variant, compiled in parallel) and the host
+scene generator into ``_lib/libpm_scene.so``.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+INC = os.path.join(ROOT, "include")
+LIB_DIR = os.path.join(PKG, "_lib")
+OBJ_DIR = os.path.join(ROOT, "_build", "obj")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + INC, "-I" + CSRC] + ARCH
+MAX_SOURCES = 10
+
+
+def _nvcc() -> str:
+    cand = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(cand):
+        raise RuntimeError("nvcc not found")
+    return cand
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("command failed: " + " ".join(cmd) + "\n" + r.stdout)
+    return r.stdout
+
+
+def _sources():
+    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
+    deps += [os.path.join(INC, f) for f in os.listdir(INC)]
+    units = []
+    for f in ("pm_api.cu", "pm_prep.cu", "pm_post.cu"):
+        units.append((os.path.join(CSRC, f), os.path.join(OBJ_DIR, f.replace(".cu", ".o")), []))
+    for s in range(1, MAX_SOURCES + 1):
+        units.append((os.path.join(CSRC, "pm_inst.cu"), os.path.join(OBJ_DIR, f"pm_inst_s{s}.o"),
+                      [f"-DPM_INST_S={s}"]))
+    return units, deps
+
+
+def _stale(obj, srcs):
+    if not os.path.exists(obj):
+        return True
+    t = os.path.getmtime(obj)
+    return any(os.path.getmtime(s) > t for s in srcs)
+
+
+def build_pm(force: bool = False, jobs: int | None = None, verbose: bool = False) -> str:
+    os.makedirs(OBJ_DIR, exist_ok=True)
+    os.makedirs(LIB_DIR, exist_ok=True)
+    nvcc = _nvcc()
+    units, deps = _sources()
+    todo = [(src, obj, extra) for src, obj, extra in units if force or _stale(obj, [src] + deps)]
+    jobs = jobs or min(len(todo) or 1, os.cpu_count() or 4)
+    with cf.ThreadPoolExecutor(max_workers=jobs) as ex:
+        futs = [ex.submit(_run, [nvcc] + NVCC_FLAGS + extra + ["-c", src, "-o", obj]) for src, obj, extra in todo]
+        for f in futs:
+            out = f.result()
+            if verbose and out.strip():
+                print(out)
+    lib = os.path.join(LIB_DIR, "libpm_gb300.so")
+    objs = [obj for _, obj, _ in units]
+    if force or todo or _stale(lib, objs):
+        _run([nvcc, "-shared"] + ARCH + ["-o", lib] + objs)
+    return lib
+
+
+def build_scene(force: bool = False) -> str:
+    os.makedirs(LIB_DIR, exist_ok=True)
+    src = os.path.join(CSRC, "scene.cpp")
+    lib = os.path.join(LIB_DIR, "libpm_scene.so")
+    if force or _stale(lib, [src, os.path.join(INC, "pm_scene.h")]):
+        _run(["g++", "-O2", "-fopenmp", "-fPIC", "-shared", "-std=c++17", "-I" + INC, "-o", lib, src])
+    return lib
+
+
+def build(force: bool = False, verbose: bool = False):
+    with cf.ThreadPoolExecutor(max_workers=2) as ex:
+        a = ex.submit(build_pm, force, None, verbose)
+        b = ex.submit(build_scene, force)
+        return a.result(), b.result()
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))

@@ -1,0 +1,891 @@
+// C ABI of the densifier (include/pm_gb300.h): contexts, device-resident
+// requests, the captured init/sweep/post-filter graph, fixed-hypothesis
+// scoring, the consistency filter and point fusion.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "pm_gb300.h"
+#include "pm_kernels.h"
+#include "pm_sweep.cuh"
+
+namespace pm {
+template <int S>
+cudaError_t configure_tile();
+}
+
+namespace {
+
+struct Trig {
+    int W = 0, H = 0;
+    float2 *row = nullptr, *col = nullptr;
+};
+
+}  // namespace
+
+struct pm_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    size_t budget = 0, used = 0;
+    std::string err;
+    uint64_t launches = 0;
+    std::vector<Trig> trig;
+    pm_request *cached = nullptr;
+    void *scratch = nullptr;
+    size_t scratch_bytes = 0;
+};
+
+struct pm_request {
+    pm_ctx *ctx = nullptr;
+    int W = 0, H = 0, S = 0;
+    pm_params prm{};
+    size_t bytes = 0;
+    void *block = nullptr;  // one device allocation holding everything below
+    float *ref = nullptr;
+    uint8_t *raw = nullptr;
+    void *quad[PM_MAX_SOURCES] = {};
+    uint8_t *mask = nullptr;
+    bool has_mask = false;
+    float4 *plane = nullptr;
+    float *score = nullptr;
+    int8_t *best = nullptr;
+    float *d0 = nullptr, *s0 = nullptr, *m1 = nullptr, *fdepth = nullptr, *fscore = nullptr;
+    float *x_depth = nullptr, *x_score = nullptr, *x_plane3 = nullptr, *x_normal3 = nullptr;
+    int32_t *x_best = nullptr;
+    double R[PM_MAX_SOURCES + 1][9] = {}, t[PM_MAX_SOURCES + 1][3] = {};
+    bool have[PM_MAX_SOURCES + 1] = {};
+    Trig trig;
+    pm::SweepArgs args{};
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    bool graph_dirty = true;
+    bool postprocessed = false;
+};
+
+namespace {
+
+int fail(pm_ctx *ctx, int code, const char *fmt, ...) {
+    if (ctx) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        ctx->err = buf;
+    }
+    return code;
+}
+
+#define PM_CUDA(ctx, call)                                                                             \
+    do {                                                                                               \
+        cudaError_t e_ = (call);                                                                       \
+        if (e_ != cudaSuccess) return fail((ctx), PM_ECUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+int get_trig(pm_ctx *ctx, int W, int H, Trig *out) {
+    for (const Trig &t : ctx->trig)
+        if (t.W == W && t.H == H) {
+            *out = t;
+            return PM_OK;
+        }
+    // lat = -pi (i/H - 1/2), lon = 2 pi (j/W - 1/2), evaluated in FP64 and rounded
+    std::vector<float2> row(H), col(W);
+    for (int i = 0; i < H; ++i) {
+        const double lat = -M_PI * ((double)i / H - 0.5);
+        row[i] = make_float2((float)std::cos(lat), (float)std::sin(lat));
+    }
+    for (int j = 0; j < W; ++j) {
+        const double lon = 2.0 * M_PI * ((double)j / W - 0.5);
+        col[j] = make_float2((float)std::sin(lon), (float)std::cos(lon));
+    }
+    Trig t;
+    t.W = W;
+    t.H = H;
+    PM_CUDA(ctx, cudaMalloc(&t.row, sizeof(float2) * H));
+    PM_CUDA(ctx, cudaMalloc(&t.col, sizeof(float2) * W));
+    PM_CUDA(ctx, cudaMemcpy(t.row, row.data(), sizeof(float2) * H, cudaMemcpyHostToDevice));
+    PM_CUDA(ctx, cudaMemcpy(t.col, col.data(), sizeof(float2) * W, cudaMemcpyHostToDevice));
+    ctx->trig.push_back(t);
+    *out = t;
+    return PM_OK;
+}
+
+int ensure_scratch(pm_ctx *ctx, size_t bytes) {
+    if (ctx->scratch_bytes >= bytes) return PM_OK;
+    if (ctx->scratch) cudaFree(ctx->scratch);
+    ctx->scratch = nullptr;
+    ctx->scratch_bytes = 0;
+    if (cudaMalloc(&ctx->scratch, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(ctx, PM_ENOMEM, "scratch allocation of %zu bytes failed", bytes);
+    }
+    ctx->scratch_bytes = bytes;
+    return PM_OK;
+}
+
+bool finite_pose(const double *R, const double *t) {
+    for (int a = 0; a < 9; ++a)
+        if (!std::isfinite(R[a])) return false;
+    for (int a = 0; a < 3; ++a)
+        if (!std::isfinite(t[a])) return false;
+    return true;
+}
+
+// X_k = M X_0 + c with M = R_k R_0^T, c = t_k - M t_0 (FP64, then rounded)
+void compose(const double *R0, const double *t0, const double *Rk, const double *tk, float *M, float *c) {
+    double Md[9];
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b)
+            Md[3 * a + b] = Rk[3 * a] * R0[3 * b] + Rk[3 * a + 1] * R0[3 * b + 1] + Rk[3 * a + 2] * R0[3 * b + 2];
+    for (int a = 0; a < 9; ++a) M[a] = (float)Md[a];
+    for (int a = 0; a < 3; ++a) c[a] = (float)(tk[a] - (Md[3 * a] * t0[0] + Md[3 * a + 1] * t0[1] + Md[3 * a + 2] * t0[2]));
+}
+
+int validate_params(pm_ctx *ctx, const pm_params *p) {
+    if (!p) return fail(ctx, PM_EINVAL, "params is NULL");
+    if (p->patch_half != 1 && p->patch_half != 3 && p->patch_half != 5)
+        return fail(ctx, PM_EINVAL, "patch_half must be 1, 3 or 5 (got %d)", p->patch_half);
+    if (p->iterations < 0 || p->iterations > 1000) return fail(ctx, PM_EINVAL, "iterations out of range");
+    if (p->combine < PM_COMBINE_FOLD || p->combine > PM_COMBINE_TOPK) return fail(ctx, PM_EINVAL, "bad combine");
+    if (p->top_k < 1) return fail(ctx, PM_EINVAL, "top_k must be >= 1");
+    if (p->seam != PM_SEAM_CLAMP && p->seam != PM_SEAM_WRAP) return fail(ctx, PM_EINVAL, "bad seam");
+    if (p->init_mode != PM_INIT_LOGUNIFORM_HEMI && p->init_mode != PM_INIT_REF_UNIFORM)
+        return fail(ctx, PM_EINVAL, "bad init_mode");
+    if (p->image_format != PM_IMAGE_U8 && p->image_format != PM_IMAGE_F16)
+        return fail(ctx, PM_EINVAL, "bad image_format");
+    if (!(p->min_depth > 0.0f) || !(p->max_depth > p->min_depth) || !std::isfinite(p->max_depth))
+        return fail(ctx, PM_EINVAL, "need 0 < min_depth < max_depth");
+    if (!(p->sigma_color > 0.0f) || !(p->sigma_x > 0.0f)) return fail(ctx, PM_EINVAL, "sigmas must be > 0");
+    if (!std::isfinite(p->min_score) || !(p->min_patch_sd >= 0.0f)) return fail(ctx, PM_EINVAL, "bad thresholds");
+    return PM_OK;
+}
+
+int validate_size(pm_ctx *ctx, int W, int H, int S) {
+    if (W < 16 || H < 16 || W > 32768 || H > 16384)
+        return fail(ctx, PM_EINVAL, "image size %dx%d out of range (16..32768 x 16..16384)", W, H);
+    if ((size_t)(W + 1) * (H + 1) >= (size_t)1 << 31) return fail(ctx, PM_EINVAL, "image too large");
+    if (S < 1 || S > PM_MAX_SOURCES) return fail(ctx, PM_EINVAL, "n_sources must be 1..%d (got %d)", PM_MAX_SOURCES, S);
+    return PM_OK;
+}
+
+void fill_args(pm_request *r) {
+    pm::SweepArgs &a = r->args;
+    const pm_params &p = r->prm;
+    for (int k = 0; k < r->S; ++k) {
+        compose(r->R[0], r->t[0], r->R[k + 1], r->t[k + 1], a.P.M[k], a.P.c[k]);
+        a.quad[k] = r->quad[k];
+    }
+    a.qpitch = r->W + 1;
+    a.row_trig = r->trig.row;
+    a.col_trig = r->trig.col;
+    a.ref = r->ref;
+    a.plane = r->plane;
+    a.score = r->score;
+    a.best = r->best;
+    a.W = r->W;
+    a.H = r->H;
+    a.Wf = (float)r->W;
+    a.Hf = (float)r->H;
+    a.patch_half = p.patch_half;
+    a.combine = p.combine;
+    a.top_k = p.top_k;
+    a.seed = p.seed;
+    a.keyframe = p.keyframe_id;
+    a.color_factor = 1.0f / (2 * p.sigma_color * p.sigma_color);
+    a.dist_factor = 1.0f / (2 * p.sigma_x * p.sigma_x);
+    float dr = 0.02f, nr = 0.5f;  // PatchMatchCuda.cu:348-349,393-394 (float *= double)
+    for (int t = 0; t < 6; ++t) {
+        a.depth_range[t] = dr;
+        a.normal_range[t] = nr;
+        dr = (float)(dr * 0.3);
+        nr = (float)(nr * 0.8);
+    }
+}
+
+int launch_tile(pm_request *r, int mode, int colour, int sweep) {
+    pm::SweepArgs a = r->args;
+    a.mode = mode;
+    a.colour = colour;
+    a.sweep = sweep;
+    cudaError_t e = pm::dispatch_tile(r->S, r->prm.image_format, pm::tile_grid(r->W, r->H), r->ctx->stream, a);
+    r->ctx->launches++;
+    if (e != cudaSuccess) return fail(r->ctx, PM_ECUDA, "tile kernel launch: %s", cudaGetErrorString(e));
+    return PM_OK;
+}
+
+int check_views(pm_request *r) {
+    for (int k = 0; k <= r->S; ++k)
+        if (!r->have[k]) return fail(r->ctx, PM_EINVAL, "view %d has not been set", k);
+    return PM_OK;
+}
+
+int enqueue_init(pm_request *r) {
+    const pm_params &p = r->prm;
+    pm::launch_init_planes(r->ctx->stream, r->trig.row, r->trig.col, r->W, r->H, p.seed, p.keyframe_id, p.init_mode,
+                           p.min_depth, p.max_depth, r->plane, r->score, r->best);
+    r->ctx->launches++;
+    for (int c = 0; c < 2; ++c) {
+        int rc = launch_tile(r, pm::kModeScore, c, 0);
+        if (rc) return rc;
+    }
+    return PM_OK;
+}
+
+int enqueue_sweeps(pm_request *r, int first_half, int n_half) {
+    for (int h = first_half; h < first_half + n_half; ++h) {
+        int rc = launch_tile(r, pm::kModeSweep, h & 1, h >> 1);
+        if (rc) return rc;
+    }
+    return PM_OK;
+}
+
+int enqueue_post(pm_request *r) {
+    pm::PostArgs a{};
+    a.plane = r->plane;
+    a.score = r->score;
+    a.ref = r->ref;
+    a.mask = r->has_mask ? r->mask : nullptr;
+    a.W = r->W;
+    a.H = r->H;
+    a.patch_half = r->prm.patch_half;
+    a.min_var = r->prm.min_patch_sd * r->prm.min_patch_sd;
+    a.min_depth = r->prm.min_depth;
+    a.max_depth = r->prm.max_depth;
+    a.min_score = r->prm.min_score;
+    a.d0 = r->d0;
+    a.s0 = r->s0;
+    a.m1 = r->m1;
+    a.out_depth = r->fdepth;
+    a.out_score = r->fscore;
+    pm::launch_postprocess(r->ctx->stream, a);
+    r->ctx->launches += 3;
+    return PM_OK;
+}
+
+int enqueue_run(pm_request *r) {
+    int rc = enqueue_init(r);
+    if (!rc) rc = enqueue_sweeps(r, 0, 2 * r->prm.iterations);
+    if (!rc && r->prm.postprocess) rc = enqueue_post(r);
+    return rc;
+}
+
+}  // namespace
+
+namespace pm {
+dim3 tile_grid(int W, int H) { return dim3((W + kTileW - 1) / kTileW, (H + kTileH - 1) / kTileH); }
+
+cudaError_t dispatch_tile(int S, int fmt, dim3 grid, cudaStream_t st, const SweepArgs &a) {
+    switch (S) {
+        case 1: return launch_tile<1>(fmt, grid, st, a);
+        case 2: return launch_tile<2>(fmt, grid, st, a);
+        case 3: return launch_tile<3>(fmt, grid, st, a);
+        case 4: return launch_tile<4>(fmt, grid, st, a);
+        case 5: return launch_tile<5>(fmt, grid, st, a);
+        case 6: return launch_tile<6>(fmt, grid, st, a);
+        case 7: return launch_tile<7>(fmt, grid, st, a);
+        case 8: return launch_tile<8>(fmt, grid, st, a);
+        case 9: return launch_tile<9>(fmt, grid, st, a);
+        case 10: return launch_tile<10>(fmt, grid, st, a);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t dispatch_hyp(int S, int fmt, int n, cudaStream_t st, const HypArgs &a) {
+    switch (S) {
+        case 1: return launch_hyp<1>(fmt, n, st, a);
+        case 2: return launch_hyp<2>(fmt, n, st, a);
+        case 3: return launch_hyp<3>(fmt, n, st, a);
+        case 4: return launch_hyp<4>(fmt, n, st, a);
+        case 5: return launch_hyp<5>(fmt, n, st, a);
+        case 6: return launch_hyp<6>(fmt, n, st, a);
+        case 7: return launch_hyp<7>(fmt, n, st, a);
+        case 8: return launch_hyp<8>(fmt, n, st, a);
+        case 9: return launch_hyp<9>(fmt, n, st, a);
+        case 10: return launch_hyp<10>(fmt, n, st, a);
+        default: return cudaErrorInvalidValue;
+    }
+}
+}  // namespace pm
+
+// ===========================================================================
+extern "C" {
+
+void pm_params_default(pm_params *p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof *p);
+    p->patch_half = 5;
+    p->iterations = 8;
+    p->combine = PM_COMBINE_FOLD;
+    p->top_k = 3;
+    p->seam = PM_SEAM_CLAMP;
+    p->init_mode = PM_INIT_LOGUNIFORM_HEMI;
+    p->image_format = PM_IMAGE_U8;
+    p->postprocess = 1;
+    p->min_depth = 0.3f;
+    p->max_depth = 20.0f;
+    p->min_score = 0.1f;
+    p->min_patch_sd = 0.0f;
+    p->sigma_color = 50.0f;
+    p->sigma_x = 5.0f;
+    p->seed = 0;
+    p->keyframe_id = 0;
+}
+
+const char *pm_status_string(int s) {
+    switch (s) {
+        case PM_OK: return "ok";
+        case PM_EINVAL: return "invalid argument";
+        case PM_ENOMEM: return "out of device memory";
+        case PM_EBUDGET: return "HBM budget exceeded";
+        case PM_ETIMEOUT: return "timed out";
+        case PM_ECUDA: return "CUDA error";
+        case PM_ENOTREADY: return "not ready";
+        case PM_ECANCELLED: return "cancelled";
+        case PM_ENOTBUILT: return "configuration not built";
+        default: return "unknown status";
+    }
+}
+
+int pm_create(int device, size_t hbm_budget_bytes, pm_ctx **out) {
+    if (!out) return PM_EINVAL;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return PM_ECUDA;
+    }
+    if (device < 0 || device >= n) return PM_EINVAL;
+    if (cudaSetDevice(device) != cudaSuccess) return PM_ECUDA;
+    pm_ctx *ctx = new pm_ctx();
+    ctx->device = device;
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete ctx;
+        return PM_ECUDA;
+    }
+    size_t fr = 0, tot = 0;
+    cudaMemGetInfo(&fr, &tot);
+    ctx->budget = hbm_budget_bytes ? hbm_budget_bytes : (size_t)(0.9 * (double)fr);
+    // opt every tile-kernel variant in to its dynamic shared memory up front,
+    // so graph capture never meets a first-use attribute call
+    cudaError_t e = cudaSuccess;
+    e = e ? e : pm::configure_tile<1>();
+    e = e ? e : pm::configure_tile<2>();
+    e = e ? e : pm::configure_tile<3>();
+    e = e ? e : pm::configure_tile<4>();
+    e = e ? e : pm::configure_tile<5>();
+    e = e ? e : pm::configure_tile<6>();
+    e = e ? e : pm::configure_tile<7>();
+    e = e ? e : pm::configure_tile<8>();
+    e = e ? e : pm::configure_tile<9>();
+    e = e ? e : pm::configure_tile<10>();
+    if (e != cudaSuccess) {
+        cudaStreamDestroy(ctx->stream);
+        delete ctx;
+        return PM_ECUDA;
+    }
+    *out = ctx;
+    return PM_OK;
+}
+
+int pm_destroy(pm_ctx *ctx) {
+    if (!ctx) return PM_EINVAL;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    if (ctx->cached) pm_request_destroy(ctx->cached);
+    for (Trig &t : ctx->trig) {
+        cudaFree(t.row);
+        cudaFree(t.col);
+    }
+    if (ctx->scratch) cudaFree(ctx->scratch);
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return PM_OK;
+}
+
+const char *pm_last_error(const pm_ctx *ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+uint64_t pm_launch_count(const pm_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+size_t pm_request_bytes(int W, int H, int S, int fmt) {
+    const size_t N = (size_t)W * H, NQ = (size_t)(W + 1) * (H + 1);
+    const size_t qb = fmt == PM_IMAGE_F16 ? 8 : 4;
+    size_t b = 0;
+    b += align256(N * 4);                 // ref
+    b += align256(N * 2);                 // raw staging
+    b += (size_t)S * align256(NQ * qb);   // quads
+    b += align256(N);                     // mask
+    b += align256(N * 16);                // plane
+    b += align256(N * 4);                 // score
+    b += align256(N);                     // best
+    b += 5 * align256(N * 4);             // d0 s0 m1 fdepth fscore
+    b += 2 * align256(N * 4) + 2 * align256(N * 12) + align256(N * 4);  // export staging
+    return b;
+}
+
+int pm_request_create(pm_ctx *ctx, int W, int H, int S, const pm_params *params, pm_request **out) {
+    if (!ctx || !out) return fail(ctx, PM_EINVAL, "NULL argument");
+    *out = nullptr;
+    int rc = validate_size(ctx, W, H, S);
+    if (rc) return rc;
+    rc = validate_params(ctx, params);
+    if (rc) return rc;
+    PM_CUDA(ctx, cudaSetDevice(ctx->device));
+    const size_t bytes = pm_request_bytes(W, H, S, params->image_format);
+    if (ctx->used + bytes > ctx->budget)
+        return fail(ctx, PM_EBUDGET, "request needs %zu bytes, %zu of %zu in use", bytes, ctx->used, ctx->budget);
+    pm_request *r = new pm_request();
+    r->ctx = ctx;
+    r->W = W;
+    r->H = H;
+    r->S = S;
+    r->prm = *params;
+    r->bytes = bytes;
+    rc = get_trig(ctx, W, H, &r->trig);
+    if (rc) {
+        delete r;
+        return rc;
+    }
+    if (cudaMalloc(&r->block, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        delete r;
+        return fail(ctx, PM_ENOMEM, "device allocation of %zu bytes failed", bytes);
+    }
+    const size_t N = (size_t)W * H, NQ = (size_t)(W + 1) * (H + 1);
+    const size_t qb = params->image_format == PM_IMAGE_F16 ? 8 : 4;
+    char *p = static_cast<char *>(r->block);
+    auto take = [&](size_t n) { void *q = p; p += align256(n); return q; };
+    r->ref = (float *)take(N * 4);
+    r->raw = (uint8_t *)take(N * 2);
+    for (int k = 0; k < S; ++k) r->quad[k] = take(NQ * qb);
+    r->mask = (uint8_t *)take(N);
+    r->plane = (float4 *)take(N * 16);
+    r->score = (float *)take(N * 4);
+    r->best = (int8_t *)take(N);
+    r->d0 = (float *)take(N * 4);
+    r->s0 = (float *)take(N * 4);
+    r->m1 = (float *)take(N * 4);
+    r->fdepth = (float *)take(N * 4);
+    r->fscore = (float *)take(N * 4);
+    r->x_depth = (float *)take(N * 4);
+    r->x_score = (float *)take(N * 4);
+    r->x_plane3 = (float *)take(N * 12);
+    r->x_normal3 = (float *)take(N * 12);
+    r->x_best = (int32_t *)take(N * 4);
+    ctx->used += bytes;
+    *out = r;
+    return PM_OK;
+}
+
+int pm_request_destroy(pm_request *r) {
+    if (!r) return PM_EINVAL;
+    pm_ctx *ctx = r->ctx;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    if (r->gexec) cudaGraphExecDestroy(r->gexec);
+    if (r->graph) cudaGraphDestroy(r->graph);
+    cudaFree(r->block);
+    ctx->used -= r->bytes;
+    if (ctx->cached == r) ctx->cached = nullptr;
+    delete r;
+    return PM_OK;
+}
+
+int pm_request_set_params(pm_request *r, const pm_params *params) {
+    if (!r) return PM_EINVAL;
+    int rc = validate_params(r->ctx, params);
+    if (rc) return rc;
+    if (params->image_format != r->prm.image_format || params->seam != r->prm.seam) {
+        for (int k = 0; k <= r->S; ++k) r->have[k] = false;  // sampling images must be rebuilt
+    }
+    r->prm = *params;
+    r->graph_dirty = true;
+    return PM_OK;
+}
+
+int pm_request_set_view(pm_request *r, int k, const pm_view *v) {
+    if (!r) return PM_EINVAL;
+    pm_ctx *ctx = r->ctx;
+    if (k < 0 || k > r->S) return fail(ctx, PM_EINVAL, "view index %d out of range 0..%d", k, r->S);
+    if (!v || !v->gray) return fail(ctx, PM_EINVAL, "view %d has no image", k);
+    if (!finite_pose(v->R_cw, v->t_cw)) return fail(ctx, PM_EINVAL, "view %d pose is not finite", k);
+    PM_CUDA(ctx, cudaSetDevice(ctx->device));
+    const size_t es = r->prm.image_format == PM_IMAGE_F16 ? 2 : 1;
+    const size_t row = (size_t)r->W * es;
+    const size_t pitch = v->pitch_bytes ? v->pitch_bytes : row;
+    if (pitch < row) return fail(ctx, PM_EINVAL, "pitch %zu smaller than a row (%zu)", pitch, row);
+    PM_CUDA(ctx, cudaMemcpy2DAsync(r->raw, row, v->gray, pitch, row, r->H, cudaMemcpyHostToDevice, ctx->stream));
+    if (k == 0) {
+        pm::launch_ref_to_float(ctx->stream, r->raw, row, r->prm.image_format, r->W, r->H, r->ref);
+        ctx->launches++;
+        r->has_mask = v->mask != nullptr;
+        if (v->mask)
+            PM_CUDA(ctx, cudaMemcpyAsync(r->mask, v->mask, (size_t)r->W * r->H, cudaMemcpyHostToDevice, ctx->stream));
+    } else {
+        pm::launch_build_quad(ctx->stream, r->raw, row, r->prm.image_format, r->W, r->H, r->prm.seam, r->quad[k - 1]);
+        ctx->launches++;
+    }
+    PM_CUDA(ctx, cudaGetLastError());
+    std::memcpy(r->R[k], v->R_cw, sizeof(double) * 9);
+    std::memcpy(r->t[k], v->t_cw, sizeof(double) * 3);
+    r->have[k] = true;
+    r->graph_dirty = true;
+    return PM_OK;
+}
+
+int pm_request_init(pm_request *r) {
+    if (!r) return PM_EINVAL;
+    int rc = check_views(r);
+    if (rc) return rc;
+    PM_CUDA(r->ctx, cudaSetDevice(r->ctx->device));
+    fill_args(r);
+    r->postprocessed = false;
+    return enqueue_init(r);
+}
+
+int pm_request_set_state(pm_request *r, const float *planes, const float *scores) {
+    if (!r || !planes) return fail(r ? r->ctx : nullptr, PM_EINVAL, "NULL argument");
+    int rc = check_views(r);
+    if (rc) return rc;
+    pm_ctx *ctx = r->ctx;
+    PM_CUDA(ctx, cudaSetDevice(ctx->device));
+    fill_args(r);
+    const size_t N = (size_t)r->W * r->H;
+    rc = ensure_scratch(ctx, N * 16);
+    if (rc) return rc;
+    float *dpl = (float *)ctx->scratch, *dsc = dpl + 3 * N;
+    PM_CUDA(ctx, cudaMemcpyAsync(dpl, planes, N * 12, cudaMemcpyHostToDevice, ctx->stream));
+    if (scores) PM_CUDA(ctx, cudaMemcpyAsync(dsc, scores, N * 4, cudaMemcpyHostToDevice, ctx->stream));
+    pm::launch_set_planes(ctx->stream, dpl, scores ? dsc : nullptr, r->trig.row, r->trig.col, r->W, r->H, r->plane,
+                          r->score, r->best);
+    ctx->launches++;
+    if (!scores)
+        for (int c = 0; c < 2; ++c) {
+            rc = launch_tile(r, pm::kModeScore, c, 0);
+            if (rc) return rc;
+        }
+    PM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    r->postprocessed = false;
+    return PM_OK;
+}
+
+int pm_request_sweep(pm_request *r, int first_half, int n_half) {
+    if (!r) return PM_EINVAL;
+    if (first_half < 0 || n_half < 0) return fail(r->ctx, PM_EINVAL, "negative half-sweep index");
+    int rc = check_views(r);
+    if (rc) return rc;
+    PM_CUDA(r->ctx, cudaSetDevice(r->ctx->device));
+    fill_args(r);
+    r->postprocessed = false;
+    return enqueue_sweeps(r, first_half, n_half);
+}
+
+int pm_request_postprocess(pm_request *r) {
+    if (!r) return PM_EINVAL;
+    PM_CUDA(r->ctx, cudaSetDevice(r->ctx->device));
+    int rc = enqueue_post(r);
+    if (!rc) r->postprocessed = true;
+    return rc;
+}
+
+int pm_request_run(pm_request *r) {
+    if (!r) return PM_EINVAL;
+    pm_ctx *ctx = r->ctx;
+    int rc = check_views(r);
+    if (rc) return rc;
+    PM_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (r->graph_dirty || !r->gexec) {
+        fill_args(r);
+        cudaGraph_t g = nullptr;
+        PM_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        const uint64_t before = ctx->launches;
+        rc = enqueue_run(r);
+        cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        if (ce != cudaSuccess) return fail(ctx, PM_ECUDA, "graph capture: %s", cudaGetErrorString(ce));
+        ctx->launches = before;  // counted again on replay below
+        bool updated = false;
+        if (r->gexec) {
+            cudaGraphExecUpdateResultInfo info;
+            if (cudaGraphExecUpdate(r->gexec, g, &info) == cudaSuccess) updated = true;
+            else cudaGetLastError();
+        }
+        if (!updated) {
+            if (r->gexec) cudaGraphExecDestroy(r->gexec);
+            r->gexec = nullptr;
+            PM_CUDA(ctx, cudaGraphInstantiate(&r->gexec, g, 0));
+        }
+        if (r->graph) cudaGraphDestroy(r->graph);
+        r->graph = g;
+        r->graph_dirty = false;
+    }
+    PM_CUDA(ctx, cudaGraphLaunch(r->gexec, ctx->stream));
+    ctx->launches += 3 + 2 * (uint64_t)r->prm.iterations + (r->prm.postprocess ? 3 : 0);
+    r->postprocessed = r->prm.postprocess != 0;
+    return PM_OK;
+}
+
+int pm_request_read(pm_request *r, pm_maps *out, int raw) {
+    if (!r || !out) return fail(r ? r->ctx : nullptr, PM_EINVAL, "NULL argument");
+    pm_ctx *ctx = r->ctx;
+    PM_CUDA(ctx, cudaSetDevice(ctx->device));
+    const size_t N = (size_t)r->W * r->H;
+    const int use_raw = raw || !r->postprocessed;
+    pm::launch_export(ctx->stream, r->plane, r->score, r->best, r->fdepth, r->fscore, r->trig.row, r->trig.col, r->W,
+                      r->H, use_raw, r->x_depth, r->x_score, r->x_plane3, r->x_normal3, r->x_best);
+    ctx->launches++;
+    if (out->depth) PM_CUDA(ctx, cudaMemcpyAsync(out->depth, r->x_depth, N * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    if (out->score) PM_CUDA(ctx, cudaMemcpyAsync(out->score, r->x_score, N * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    if (out->plane) PM_CUDA(ctx, cudaMemcpyAsync(out->plane, r->x_plane3, N * 12, cudaMemcpyDeviceToHost, ctx->stream));
+    if (out->normal)
+        PM_CUDA(ctx, cudaMemcpyAsync(out->normal, r->x_normal3, N * 12, cudaMemcpyDeviceToHost, ctx->stream));
+    if (out->best_view)
+        PM_CUDA(ctx, cudaMemcpyAsync(out->best_view, r->x_best, N * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    PM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return PM_OK;
+}
+
+int pm_request_synchronize(pm_request *r) {
+    if (!r) return PM_EINVAL;
+    PM_CUDA(r->ctx, cudaStreamSynchronize(r->ctx->stream));
+    return PM_OK;
+}
+
+const float *pm_request_depth_device(const pm_request *r) { return r ? r->fdepth : nullptr; }
+
+int pm_densify(pm_ctx *ctx, int W, int H, const pm_view *views, int n_views, const pm_params *params, pm_maps *out) {
+    if (!ctx || !views || !out || !out->depth) return fail(ctx, PM_EINVAL, "NULL argument");
+    const int S = n_views - 1;
+    int rc = validate_size(ctx, W, H, S);
+    if (rc) return rc;
+    rc = validate_params(ctx, params);
+    if (rc) return rc;
+    pm_request *r = ctx->cached;
+    if (r && (r->W != W || r->H != H || r->S != S || r->prm.image_format != params->image_format)) {
+        pm_request_destroy(r);
+        r = nullptr;
+    }
+    if (!r) {
+        rc = pm_request_create(ctx, W, H, S, params, &r);
+        if (rc) return rc;
+        ctx->cached = r;
+    }
+    rc = pm_request_set_params(r, params);
+    for (int k = 0; !rc && k < n_views; ++k) rc = pm_request_set_view(r, k, &views[k]);
+    if (!rc) rc = pm_request_run(r);
+    if (!rc) rc = pm_request_read(r, out, 0);
+    return rc;
+}
+
+int pm_score_hypotheses(pm_request *r, int n, const int32_t *ij, const float *planes, float *scores, int32_t *best,
+                        float *per_source) {
+    if (!r) return PM_EINVAL;
+    pm_ctx *ctx = r->ctx;
+    if (n < 0 || (n > 0 && (!ij || !planes))) return fail(ctx, PM_EINVAL, "bad hypothesis arrays");
+    if (n == 0) return PM_OK;
+    int rc = check_views(r);
+    if (rc) return rc;
+    const int ph = r->prm.patch_half;
+    for (int h = 0; h < n; ++h) {
+        const int i = ij[2 * h], j = ij[2 * h + 1];
+        if (i < ph || i >= r->H - ph || j < ph || j >= r->W - ph)
+            return fail(ctx, PM_EINVAL, "hypothesis %d at (%d, %d) has taps outside the image", h, i, j);
+    }
+    PM_CUDA(ctx, cudaSetDevice(ctx->device));
+    fill_args(r);
+    const size_t S = (size_t)r->S;
+    const size_t need = align256((size_t)n * 8) + align256((size_t)n * 12) + align256((size_t)n * 4) * 2 +
+                        align256((size_t)n * 4 * S);
+    rc = ensure_scratch(ctx, need);
+    if (rc) return rc;
+    char *p = (char *)ctx->scratch;
+    int2 *dij = (int2 *)p;
+    p += align256((size_t)n * 8);
+    float *dpl = (float *)p;
+    p += align256((size_t)n * 12);
+    float *dsc = (float *)p;
+    p += align256((size_t)n * 4);
+    int *dbest = (int *)p;
+    p += align256((size_t)n * 4);
+    float *dper = (float *)p;
+    PM_CUDA(ctx, cudaMemcpyAsync(dij, ij, (size_t)n * 8, cudaMemcpyHostToDevice, ctx->stream));
+    PM_CUDA(ctx, cudaMemcpyAsync(dpl, planes, (size_t)n * 12, cudaMemcpyHostToDevice, ctx->stream));
+    pm::HypArgs a{};
+    a.P = r->args.P;
+    for (int k = 0; k < r->S; ++k) a.quad[k] = r->quad[k];
+    a.qpitch = r->W + 1;
+    a.row_trig = r->trig.row;
+    a.col_trig = r->trig.col;
+    a.ref = r->ref;
+    a.W = r->W;
+    a.H = r->H;
+    a.Wf = (float)r->W;
+    a.Hf = (float)r->H;
+    a.patch_half = ph;
+    a.combine = r->prm.combine;
+    a.top_k = r->prm.top_k;
+    a.color_factor = r->args.color_factor;
+    a.dist_factor = r->args.dist_factor;
+    a.n = n;
+    a.ij = dij;
+    a.planes = dpl;
+    a.scores = dsc;
+    a.best = dbest;
+    a.per_source = per_source ? dper : nullptr;
+    cudaError_t e = pm::dispatch_hyp(r->S, r->prm.image_format, n, ctx->stream, a);
+    ctx->launches++;
+    if (e != cudaSuccess) return fail(ctx, PM_ECUDA, "hypothesis kernel: %s", cudaGetErrorString(e));
+    if (scores) PM_CUDA(ctx, cudaMemcpyAsync(scores, dsc, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    if (best) PM_CUDA(ctx, cudaMemcpyAsync(best, dbest, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    if (per_source)
+        PM_CUDA(ctx, cudaMemcpyAsync(per_source, dper, (size_t)n * 4 * S, cudaMemcpyDeviceToHost, ctx->stream));
+    PM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return PM_OK;
+}
+
+int pm_filter_consistency(pm_ctx *ctx, int W, int H, int n, const float *const *depths, const double *R,
+                          const double *t, int center, float thr, int min_consistent, float reproj_px, float *out) {
+    if (!ctx || !depths || !R || !t || !out) return fail(ctx, PM_EINVAL, "NULL argument");
+    if (W < 2 || H < 2 || n < 1 || n > pm::kMaxFilterViews || center < 0 || center >= n)
+        return fail(ctx, PM_EINVAL, "bad sizes (W=%d H=%d n=%d center=%d)", W, H, n, center);
+    for (int k = 0; k < n; ++k)
+        if (!depths[k] || !finite_pose(R + 9 * k, t + 3 * k)) return fail(ctx, PM_EINVAL, "view %d invalid", k);
+    if (!(thr > 0.0f)) return fail(ctx, PM_EINVAL, "same_depth_threshold must be > 0");
+    PM_CUDA(ctx, cudaSetDevice(ctx->device));
+    Trig tr;
+    int rc = get_trig(ctx, W, H, &tr);
+    if (rc) return rc;
+    const size_t N = (size_t)W * H;
+    rc = ensure_scratch(ctx, (size_t)(n + 1) * align256(N * 4) + 256);
+    if (rc) return rc;
+    char *base = (char *)ctx->scratch;
+    std::vector<const float *> dptr(n);
+    // view order on the device: centre first, then the others in order
+    std::vector<int> order;
+    order.push_back(center);
+    for (int k = 0; k < n; ++k)
+        if (k != center) order.push_back(k);
+    for (int s = 0; s < n; ++s) {
+        float *d = (float *)(base + (size_t)s * align256(N * 4));
+        PM_CUDA(ctx, cudaMemcpyAsync(d, depths[order[s]], N * 4, cudaMemcpyHostToDevice, ctx->stream));
+        dptr[s] = d;
+    }
+    float *dout = (float *)(base + (size_t)n * align256(N * 4));
+    const float **dlist = nullptr;
+    PM_CUDA(ctx, cudaMallocAsync((void **)&dlist, sizeof(float *) * n, ctx->stream));
+    PM_CUDA(ctx, cudaMemcpyAsync(dlist, dptr.data(), sizeof(float *) * n, cudaMemcpyHostToDevice, ctx->stream));
+    pm::CleanArgs a{};
+    a.depths = dlist;
+    a.n = n;
+    a.W = W;
+    a.H = H;
+    const double *R0 = R + 9 * center, *t0 = t + 3 * center;
+    for (int s = 1; s < n; ++s) {
+        const int k = order[s];
+        compose(R0, t0, R + 9 * k, t + 3 * k, a.M[s], a.c[s]);
+        compose(R + 9 * k, t + 3 * k, R0, t0, a.Minv[s], a.cinv[s]);
+    }
+    a.row_trig = tr.row;
+    a.col_trig = tr.col;
+    a.thr = thr;
+    a.min_consistent = min_consistent;
+    a.reproj_px = reproj_px;
+    a.out = dout;
+    pm::launch_clean(ctx->stream, a);
+    ctx->launches++;
+    PM_CUDA(ctx, cudaGetLastError());
+    PM_CUDA(ctx, cudaMemcpyAsync(out, dout, N * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    PM_CUDA(ctx, cudaFreeAsync(dlist, ctx->stream));
+    PM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return PM_OK;
+}
+
+int pm_fuse(pm_ctx *ctx, int W, int H, int n, float *const *depths, const double *R, const double *t,
+            const uint8_t *bgr, float thr, float *pruned, pm_points *out) {
+    if (!ctx || !depths || !R || !t || !pruned || !out) return fail(ctx, PM_EINVAL, "NULL argument");
+    if (W < 2 || H < 2 || n < 1 || n > pm::kMaxFilterViews) return fail(ctx, PM_EINVAL, "bad sizes");
+    for (int k = 0; k < n; ++k)
+        if (!depths[k] || !finite_pose(R + 9 * k, t + 3 * k)) return fail(ctx, PM_EINVAL, "view %d invalid", k);
+    PM_CUDA(ctx, cudaSetDevice(ctx->device));
+    Trig tr;
+    int rc = get_trig(ctx, W, H, &tr);
+    if (rc) return rc;
+    const size_t N = (size_t)W * H;
+    const int nb = (int)((N + 1023) / 1024);
+    const size_t need = (size_t)n * align256(N * 4) + align256(N) + align256(N * 4) + align256(N) + align256(N * 4) +
+                        align256(N * 4) + align256((size_t)(nb + 1) * 4) + align256(N * 3) + align256(N * 12) +
+                        align256(N * 3) + align256(N * 8) + 256;
+    rc = ensure_scratch(ctx, need);
+    if (rc) return rc;
+    char *p = (char *)ctx->scratch;
+    auto take = [&](size_t b) { void *q = p; p += align256(b); return q; };
+    std::vector<float *> dptr(n);
+    for (int k = 0; k < n; ++k) {
+        dptr[k] = (float *)take(N * 4);
+        PM_CUDA(ctx, cudaMemcpyAsync(dptr[k], depths[k], N * 4, cudaMemcpyHostToDevice, ctx->stream));
+    }
+    pm::FuseArgs a{};
+    a.alive = (uint8_t *)take(N);
+    a.target = (int *)take(N * 4);
+    a.cls = (int8_t *)take(N);
+    a.first = (unsigned *)take(N * 4);
+    a.pruned = (float *)take(N * 4);
+    a.block_counts = (unsigned *)take((size_t)(nb + 1) * 4);
+    uint8_t *dbgr = (uint8_t *)take(N * 3);
+    a.xyz = (float *)take(N * 12);
+    a.bgr_out = (uint8_t *)take(N * 3);
+    a.ij_out = (int *)take(N * 8);
+    a.count = (unsigned *)take(4);
+    if (bgr) PM_CUDA(ctx, cudaMemcpyAsync(dbgr, bgr, N * 3, cudaMemcpyHostToDevice, ctx->stream));
+    a.bgr = bgr ? dbgr : nullptr;
+    float **dlist = nullptr;
+    PM_CUDA(ctx, cudaMallocAsync((void **)&dlist, sizeof(float *) * n, ctx->stream));
+    PM_CUDA(ctx, cudaMemcpyAsync(dlist, dptr.data(), sizeof(float *) * n, cudaMemcpyHostToDevice, ctx->stream));
+    a.depths = dlist;
+    a.n = n;
+    a.W = W;
+    a.H = H;
+    for (int k = 1; k < n; ++k) compose(R, t, R + 9 * k, t + 3 * k, a.M[k], a.c[k]);
+    for (int r0 = 0; r0 < 3; ++r0) {
+        for (int c0 = 0; c0 < 3; ++c0) a.Rinv[3 * r0 + c0] = (float)R[3 * c0 + r0];
+        a.tw[r0] = (float)(-(R[r0] * t[0] + R[3 + r0] * t[1] + R[6 + r0] * t[2]));
+    }
+    a.row_trig = tr.row;
+    a.col_trig = tr.col;
+    a.thr = thr;
+    pm::launch_fuse(ctx->stream, a);
+    ctx->launches += 1 + 2 * (uint64_t)(n - 1) + 3;
+    PM_CUDA(ctx, cudaGetLastError());
+    unsigned count = 0;
+    PM_CUDA(ctx, cudaMemcpyAsync(&count, a.count, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    PM_CUDA(ctx, cudaMemcpyAsync(pruned, a.pruned, N * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    for (int k = 1; k < n; ++k)
+        PM_CUDA(ctx, cudaMemcpyAsync(depths[k], dptr[k], N * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    PM_CUDA(ctx, cudaFreeAsync(dlist, ctx->stream));
+    PM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    const int m = (int)std::min<unsigned>(count, out->capacity > 0 ? (unsigned)out->capacity : 0u);
+    if (m > 0) {
+        std::vector<float> xyz((size_t)m * 3);
+        PM_CUDA(ctx, cudaMemcpy(xyz.data(), a.xyz, (size_t)m * 12, cudaMemcpyDeviceToHost));
+        if (out->xyz)
+            for (size_t q = 0; q < (size_t)m * 3; ++q) out->xyz[q] = xyz[q];
+        if (out->bgr && bgr) PM_CUDA(ctx, cudaMemcpy(out->bgr, a.bgr_out, (size_t)m * 3, cudaMemcpyDeviceToHost));
+        if (out->ij) PM_CUDA(ctx, cudaMemcpy(out->ij, a.ij_out, (size_t)m * 8, cudaMemcpyDeviceToHost));
+    }
+    out->count = (int)count;
+    if ((int)count > out->capacity)
+        return fail(ctx, PM_EINVAL, "point capacity %d too small for %u points", out->capacity, count);
+    return PM_OK;
+}
+
+}  // extern "C"

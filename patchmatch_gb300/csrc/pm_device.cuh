@@ -1,0 +1,253 @@
+// Device-side building blocks of the densifier: counter-based random numbers,
+// equirectangular angle evaluation, quad-packed bilinear sampling and the
+// per-tap NCC moment accumulation shared by every cost kernel.
+#pragma once
+
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "pm_types.h"
+
+namespace pm {
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy
+// as 1, 2, 3", SC'11).  Key = (seed, keyframe); counter = (pixel, tag, draw,
+// constant).  tag 0 = initialisation, tag s+1 = the pixel's visit in sweep s.
+// Replaces the clock-seeded cuRAND XORWOW states of the reference
+// (PatchMatchCuda.cu:246-252), which made runs irreproducible.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        if (r) { k.x += 0x9E3779B9u; k.y += 0xBB67AE85u; }
+        const uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+        const uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+        c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+    }
+    return c;
+}
+
+__device__ __forceinline__ uint4 philox_block(uint32_t seed, uint32_t kf, uint32_t pixel, uint32_t tag,
+                                              uint32_t draw) {
+    return philox4x32_10(make_uint4(pixel, tag, draw, 0x504d4742u), make_uint2(seed, kf));
+}
+
+// 24-bit uniform in (0, 1), exactly representable.
+__device__ __forceinline__ float u24(uint32_t x) {
+    return __fmul_rn(__fadd_rn((float)(x >> 8), 0.5f), 1.0f / 16777216.0f);
+}
+
+// Box-Muller pair from two words.
+__device__ __forceinline__ float2 box_muller(uint32_t a, uint32_t b) {
+    const float u1 = u24(a), u2 = u24(b);
+    const float r = sqrtf(__fmul_rn(-2.0f, logf(u1)));
+    const float th = __fmul_rn(6.28318530717958647692f, u2);
+    return make_float2(__fmul_rn(r, cosf(th)), __fmul_rn(r, sinf(th)));
+}
+
+// ---------------------------------------------------------------------------
+// atan on [0, 1]: atan(t) ~ t * P(t^2), P of degree 7, a minimax (Remez
+// exchange) fit made for this project (max error 3.7e-8 rad before float
+// rounding).  The two coefficient sets below are that polynomial scaled to
+// turns (1/2pi, longitude) and half turns (1/pi, latitude) so the angles come
+// out directly in image-fraction units.
+// ---------------------------------------------------------------------------
+#define PM_ATAN_C0 0.9999993443489075f
+#define PM_ATAN_C1 -0.33329859375953674f
+#define PM_ATAN_C2 0.19946566224098206f
+#define PM_ATAN_C3 -0.1390862911939621f
+#define PM_ATAN_C4 0.0964219719171524f
+#define PM_ATAN_C5 -0.0559123270213604f
+#define PM_ATAN_C6 0.021862957626581192f
+#define PM_ATAN_C7 -0.004054567310959101f
+
+template <int kScaleInvPi>  // 1: scale by 1/pi; 2: scale by 1/(2 pi)
+__device__ __forceinline__ float atan01_scaled(float t) {
+    constexpr float s = kScaleInvPi == 1 ? 0.318309886183790671538f : 0.159154943091895335769f;
+    const float x2 = t * t;
+    float p = PM_ATAN_C7 * s;
+    p = fmaf(p, x2, PM_ATAN_C6 * s);
+    p = fmaf(p, x2, PM_ATAN_C5 * s);
+    p = fmaf(p, x2, PM_ATAN_C4 * s);
+    p = fmaf(p, x2, PM_ATAN_C3 * s);
+    p = fmaf(p, x2, PM_ATAN_C2 * s);
+    p = fmaf(p, x2, PM_ATAN_C1 * s);
+    p = fmaf(p, x2, PM_ATAN_C0 * s);
+    return p * t;
+}
+
+// atan2(x, z) / (2 pi) in [-1/2, 1/2]: the equirectangular longitude of
+// direction (x, ., z) as a fraction of the image width (PatchMatchCuda.cu:140,143).
+__device__ __forceinline__ float lon_turns(float x, float z) {
+    const float ax = fabsf(x), az = fabsf(z);
+    const float mx = fmaxf(fmaxf(ax, az), 1e-30f), mn = fminf(ax, az);
+    const float t = __fdividef(mn, mx);
+    float a = atan01_scaled<2>(t);
+    a = (ax > az) ? 0.25f - a : a;
+    a = (z < 0.0f) ? 0.5f - a : a;
+    return copysignf(a, x);
+}
+
+// asin(y / |(x, y, z)|) / pi in [-1/2, 1/2]: minus the equirectangular
+// latitude as a fraction of the image height (PatchMatchCuda.cu:139,144),
+// evaluated as atan2(y, sqrt(x^2 + z^2)).
+__device__ __forceinline__ float lat_halfturns(float x, float y, float z) {
+    const float r2 = fmaxf(fmaf(x, x, z * z), 1e-30f);
+    const float tq = fabsf(y) * rsqrtf(r2);
+    const float t = fminf(tq, __fdividef(1.0f, tq));
+    float a = atan01_scaled<1>(t);
+    a = (tq > 1.0f) ? 0.5f - a : a;
+    return copysignf(a, y);
+}
+
+// ---------------------------------------------------------------------------
+// Quad-packed source images.  Entry (y, x) of a (H+1) x (W+1) array holds the
+// 2x2 bilinear footprint {T(x,y), T(x+1,y), T(x,y+1), T(x+1,y+1)} with the
+// border policy baked in (x+1 clamps at W-1 or wraps to 0; y+1 clamps), so a
+// sample is one aligned load.  Texel k sits at coordinate k, matching the
+// reference's texture reads at u + 0.5 (PatchMatchCuda.cu:146).
+// ---------------------------------------------------------------------------
+struct QuadU8 {
+    // shift: value subtracted from every texel, given as 2^23 + I_c so the
+    // byte-to-float conversion and the centring are one subtraction.
+    static __device__ __forceinline__ float shift_for(float centre) { return 8388608.0f + centre; }
+    static __device__ __forceinline__ float sample(const void *base, int pitch, float u, float v, float shift) {
+        // u in [0, W], v in [0, H] by construction of the angle functions
+        const float fx = floorf(u), fy = floorf(v);
+        const float ax = u - fx, ay = v - fy;
+        const int x0 = (int)fx, y0 = (int)fy;
+        const uint32_t w = __ldg(static_cast<const uint32_t *>(base) + ((size_t)y0 * pitch + x0));
+        // bytes -> floats minus the centre intensity: (2^23 + byte) - (2^23 + c)
+        const float t00 = __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540)) - shift;
+        const float t01 = __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7541)) - shift;
+        const float t10 = __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7542)) - shift;
+        const float t11 = __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7543)) - shift;
+        const float a = fmaf(ax, t01 - t00, t00);
+        const float b = fmaf(ax, t11 - t10, t10);
+        return fmaf(ay, b - a, a);
+    }
+};
+
+struct QuadF16 {
+    static __device__ __forceinline__ float shift_for(float centre) { return centre; }
+    static __device__ __forceinline__ float sample(const void *base, int pitch, float u, float v, float shift) {
+        const float fx = floorf(u), fy = floorf(v);
+        const float ax = u - fx, ay = v - fy;
+        const int x0 = (int)fx, y0 = (int)fy;
+        const uint2 w = __ldg(static_cast<const uint2 *>(base) + ((size_t)y0 * pitch + x0));
+        const float2 r0 = __half22float2(*reinterpret_cast<const __half2 *>(&w.x));
+        const float2 r1 = __half22float2(*reinterpret_cast<const __half2 *>(&w.y));
+        const float t00 = r0.x - shift, t01 = r0.y - shift, t10 = r1.x - shift, t11 = r1.y - shift;
+        const float a = fmaf(ax, t01 - t00, t00);
+        const float b = fmaf(ax, t11 - t10, t10);
+        return fmaf(ay, b - a, a);
+    }
+};
+
+// ---------------------------------------------------------------------------
+// One tap of the plane-induced warp for all S sources (PatchMatchCuda.cu:107-157,
+// restructured).  The reference maps X_c = b / (pi . b) through
+// R_r (R_1^T X_c - R_1^T t_1) + t_r and normalises.  Only the direction of the
+// source-frame point matters, so with M_r = R_r R_1^T and c_r = t_r - M_r t_1
+// (composed in FP64 on the host) we evaluate |s| * X_r = M_r (sign(s) b) + |s| c_r,
+// s = pi . b, which has the same direction and no division.
+// Moments are accumulated shifted by the centre intensity (y - I_c), which is
+// exact algebra for the NCC and avoids float cancellation in the variances.
+// ---------------------------------------------------------------------------
+template <int S, class Img>
+struct TapAccum {
+    float swy[S], swyy[S], swxy[S];
+    __device__ __forceinline__ void zero() {
+#pragma unroll
+        for (int r = 0; r < S; ++r) swy[r] = swyy[r] = swxy[r] = 0.0f;
+    }
+    // P, quad, qpitch live in kernel parameter space; b: tap bearing,
+    // w: bilateral weight, xs: tap intensity minus centre.
+    __device__ __forceinline__ void add(const PmPoses &P, const void *const *quad, int qpitch, float Wf, float Hf,
+                                        float halfW, float halfH, float shift, float px, float py, float pz,
+                                        float bx, float by, float bz, float w, float xs) {
+        const float s = fmaf(px, bx, fmaf(py, by, pz * bz));
+        const float as = fabsf(s);
+        const uint32_t sg = __float_as_uint(s) & 0x80000000u;
+        const float sbx = __uint_as_float(__float_as_uint(bx) ^ sg);
+        const float sby = __uint_as_float(__float_as_uint(by) ^ sg);
+        const float sbz = __uint_as_float(__float_as_uint(bz) ^ sg);
+#pragma unroll
+        for (int r = 0; r < S; ++r) {
+            const float X = fmaf(P.M[r][0], sbx, fmaf(P.M[r][1], sby, fmaf(P.M[r][2], sbz, as * P.c[r][0])));
+            const float Y = fmaf(P.M[r][3], sbx, fmaf(P.M[r][4], sby, fmaf(P.M[r][5], sbz, as * P.c[r][1])));
+            const float Z = fmaf(P.M[r][6], sbx, fmaf(P.M[r][7], sby, fmaf(P.M[r][8], sbz, as * P.c[r][2])));
+            const float u = fmaf(Wf, lon_turns(X, Z), halfW);
+            const float v = fmaf(Hf, lat_halfturns(X, Y, Z), halfH);
+            const float y = Img::sample(quad[r], qpitch, u, v, shift);
+            const float wy = w * y;
+            swy[r] += wy;
+            swyy[r] = fmaf(wy, y, swyy[r]);
+            swxy[r] = fmaf(wy, xs, swxy[r]);
+        }
+    }
+};
+
+// NCC from shifted moments (PatchMatchCuda.cu:161-170): -1 when either
+// weighted variance is below 0.1.
+__device__ __forceinline__ float ncc_from_moments(float sw, float swx, float swxx, float swy, float swyy,
+                                                  float swxy) {
+    const float prob = 1.0f / sw;
+    const float mx = swx * prob, my = swy * prob;
+    const float vx = fmaf(-mx, mx, swxx * prob);
+    const float vy = fmaf(-my, my, swyy * prob);
+    const float cov = fmaf(-mx, my, swxy * prob);
+    const float ncc = cov / sqrtf(vx * vy);
+    return (vx < 0.1f || vy < 0.1f) ? -1.0f : ncc;
+}
+
+// View combination of S per-source scores; best = argmax source.
+//  PM_COMBINE_FOLD: the reference's running "average when within 25 %, else
+//    max", starting from -1 (PatchMatchCuda.cu:93,171), folded over sources in order;
+//  PM_COMBINE_MAX: maximum (the reference CPU path, depthmap.cc:1104-1127);
+//  PM_COMBINE_TOPK: mean of the top_k best sources (per-pixel view selection).
+template <int S>
+__device__ __forceinline__ float combine_scores(const float (&ncc)[S], int mode, int top_k, int *best) {
+    int b = 0;
+#pragma unroll
+    for (int r = 1; r < S; ++r) b = (ncc[r] > ncc[b]) ? r : b;
+    *best = b;
+    if (mode == PM_COMBINE_MAX) {
+        float m = ncc[0];
+#pragma unroll
+        for (int r = 1; r < S; ++r) m = fmaxf(m, ncc[r]);
+        return m;
+    }
+    if (mode == PM_COMBINE_TOPK) {
+        // sum of the k largest: repeated selection over a small register array
+        float v[S];
+#pragma unroll
+        for (int r = 0; r < S; ++r) v[r] = ncc[r];
+        const int k = top_k < 1 ? 1 : (top_k > S ? S : top_k);
+        float accf = 0.0f;  // summed in descending order
+        for (int a = 0; a < k; ++a) {
+            int bi = 0;
+#pragma unroll
+            for (int r = 1; r < S; ++r) bi = (v[r] > v[bi]) ? r : bi;
+            float m = v[0];
+#pragma unroll
+            for (int r = 0; r < S; ++r) m = (r == bi) ? v[r] : m;
+            accf += m;
+#pragma unroll
+            for (int r = 0; r < S; ++r) v[r] = (r == bi) ? -3.0e38f : v[r];
+        }
+        return accf / (float)k;
+    }
+    float score = -1.0f;
+#pragma unroll
+    for (int r = 0; r < S; ++r) {
+        const float s2 = ncc[r];
+        score = (fabsf(__fdiv_rn(__fsub_rn(score, s2), s2)) < 0.25f) ? __fmul_rn(0.5f, __fadd_rn(score, s2))
+                                                                     : fmaxf(score, s2);
+    }
+    return score;
+}
+
+}  // namespace pm

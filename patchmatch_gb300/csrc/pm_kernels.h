@@ -1,0 +1,86 @@
+// Host-side launch wrappers of the densifier kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "pm_types.h"
+
+namespace pm {
+
+// pm_prep.cu
+void launch_ref_to_float(cudaStream_t st, const uint8_t *raw, size_t pitch, int fmt, int W, int H, float *out);
+void launch_build_quad(cudaStream_t st, const uint8_t *raw, size_t pitch, int fmt, int W, int H, int seam,
+                       void *quad);
+void launch_init_planes(cudaStream_t st, const float2 *row_trig, const float2 *col_trig, int W, int H, uint32_t seed,
+                        uint32_t kf, int mode, float dmin, float dmax, float4 *plane, float *score, int8_t *best);
+void launch_set_planes(cudaStream_t st, const float *planes3, const float *scores, const float2 *row_trig,
+                       const float2 *col_trig, int W, int H, float4 *plane, float *score, int8_t *best);
+
+// pm_inst.cu (one translation unit per source count S)
+template <int S>
+cudaError_t launch_tile(int fmt, dim3 grid, cudaStream_t st, const SweepArgs &a);
+template <int S>
+cudaError_t launch_hyp(int fmt, int n, cudaStream_t st, const HypArgs &a);
+cudaError_t dispatch_tile(int S, int fmt, dim3 grid, cudaStream_t st, const SweepArgs &a);
+cudaError_t dispatch_hyp(int S, int fmt, int n, cudaStream_t st, const HypArgs &a);
+dim3 tile_grid(int W, int H);
+
+// pm_post.cu
+struct PostArgs {
+    const float4 *plane;
+    const float *score;
+    const float *ref;
+    const uint8_t *mask;  // may be null
+    int W, H, patch_half;
+    float min_var, min_depth, max_depth, min_score;
+    float *d0, *s0, *m1;  // scratch: windowed depth, score, first median
+    float *out_depth, *out_score;
+};
+void launch_postprocess(cudaStream_t st, const PostArgs &a);
+// raw = 1: export the sweep state instead of the filtered maps
+void launch_export(cudaStream_t st, const float4 *plane, const float *score, const int8_t *best,
+                   const float *filt_depth, const float *filt_score, const float2 *row_trig, const float2 *col_trig,
+                   int W, int H, int raw, float *depth, float *score_out, float *plane3, float *normal3,
+                   int32_t *best32);
+
+struct CleanArgs {
+    const float *const *depths;  // device array of n device pointers; view 0 = centre
+    int n, W, H;
+    float M[PM_MAX_SOURCES + 6][9];  // centre camera -> view k (k >= 1)
+    float c[PM_MAX_SOURCES + 6][3];
+    float Minv[PM_MAX_SOURCES + 6][9];  // view k -> centre camera (round trip)
+    float cinv[PM_MAX_SOURCES + 6][3];
+    const float2 *row_trig, *col_trig;
+    float thr;
+    int min_consistent;
+    float reproj_px;
+    float *out;
+};
+constexpr int kMaxFilterViews = PM_MAX_SOURCES + 6;
+void launch_clean(cudaStream_t st, const CleanArgs &a);
+
+struct FuseArgs {
+    float *const *depths;  // device array of n device pointers; view 0 = head
+    int n, W, H;
+    float M[kMaxFilterViews][9];  // head camera -> view k
+    float c[kMaxFilterViews][3];
+    float Rinv[9], tw[3];          // head camera -> world: X_w = R0^T (X_c - t0)
+    const float2 *row_trig, *col_trig;
+    float thr;
+    uint8_t *alive;                // H*W scratch
+    int *target;                   // H*W scratch
+    int8_t *cls;                   // H*W scratch
+    unsigned *first;               // H*W scratch
+    float *pruned;                 // H*W out
+    // compaction
+    unsigned *block_counts;        // ceil(H*W / 1024) + 1
+    const uint8_t *bgr;            // H*W*3 or null
+    float *xyz;                    // out, capacity*3
+    uint8_t *bgr_out;              // out
+    int *ij_out;                   // out
+    unsigned *count;               // out (device)
+};
+void launch_fuse(cudaStream_t st, const FuseArgs &a);
+
+}  // namespace pm

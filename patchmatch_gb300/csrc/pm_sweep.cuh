@@ -1,0 +1,244 @@
+// Tile kernel of the densifier: scores each pixel's own plane (init scoring,
+// PatchMatchCuda.cu:255-270) or performs one red/black half-sweep of
+// propagation + random refinement (PatchMatchCuda.cu:273-407).
+//
+// Layout: a CTA of 256 threads owns an 8-row x 64-column image tile and
+// updates its 256 pixels of the active colour (one warp per row, one lane per
+// pixel).  All window taps of a pixel of colour c are themselves pixels of
+// colour c, so the CTA stages only those: an 18 x 37 shared-memory tile of
+// (bearing, intensity) float4 including the 5-pixel halo, indexed so that the
+// 32 lanes of a warp read 32 consecutive entries.  Per-pixel bilateral weights
+// and the hypothesis-independent reference moments are computed once per
+// visit; the inner loop then evaluates each hypothesis over the 36 taps and S
+// sources with S independent accumulation chains.
+#pragma once
+
+#include "pm_device.cuh"
+
+namespace pm {
+
+constexpr int kTileW = 64;
+constexpr int kTileH = 8;
+constexpr int kThreads = kTileH * 32;
+constexpr int kHaloMax = 5;                       // largest supported patch_half
+constexpr int kTileRows = kTileH + 2 * kHaloMax;  // 18
+constexpr int kTileCols = (kTileW + 2 * kHaloMax) / 2;  // 37 same-colour entries per row
+constexpr int kMaxTaps = (kHaloMax + 1) * (kHaloMax + 1);
+
+// Stage the same-colour (bearing, intensity) tile.  Entry (tr, cc) holds image
+// pixel (R, C) = (i0 - 5 + tr, x0 - 5 + 2 cc + ((R + colour + 1) & 1)).
+__device__ __forceinline__ void load_tile(float4 *tile, const float2 *row_trig, const float2 *col_trig,
+                                          const float *ref, int W, int H, int i0, int x0, int colour) {
+    for (int e = threadIdx.x; e < kTileRows * kTileCols; e += blockDim.x) {
+        const int tr = e / kTileCols, cc = e - tr * kTileCols;
+        const int R = i0 - kHaloMax + tr;
+        const int C = x0 - kHaloMax + 2 * cc + ((R + colour + 1) & 1);
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (R >= 0 && R < H && C >= 0 && C < W) {
+            const float2 rt = row_trig[R], ct = col_trig[C];
+            v = make_float4(rt.x * ct.x, -rt.y, rt.x * ct.y, ref[(size_t)R * W + C]);
+        }
+        tile[e] = v;
+    }
+}
+
+// Dynamic shared memory of tile_kernel: tile + weights + refinement normals.
+constexpr size_t kTileSmemBytes =
+    sizeof(float4) * kTileRows * kTileCols + sizeof(float) * (kMaxTaps + 18) * kThreads;
+
+template <int S, class Img>
+__global__ void __launch_bounds__(kThreads, 3) tile_kernel(const __grid_constant__ SweepArgs a) {
+    extern __shared__ float4 smem_f4[];
+    float4 *tile = smem_f4;
+    float *wsm = reinterpret_cast<float *>(smem_f4 + kTileRows * kTileCols);
+    float *nsm = wsm + kMaxTaps * kThreads;
+
+    const int tid = threadIdx.x, lane = tid & 31, ty = tid >> 5;
+    const int x0 = blockIdx.x * kTileW, i0 = blockIdx.y * kTileH;
+    load_tile(tile, a.row_trig, a.col_trig, a.ref, a.W, a.H, i0, x0, a.colour);
+    __syncthreads();
+
+    const int W = a.W, H = a.H, ph = a.patch_half;
+    const int i = i0 + ty;
+    const int p = (i + a.colour) & 1;
+    const int j = x0 + 2 * lane + p;
+    if (i < ph + 1 || i > H - ph - 1 || j < ph + 1 || j > W - ph - 1) return;  // PatchMatchCuda.cu:283
+
+    const float4 ctr = tile[(ty + kHaloMax) * kTileCols + ((2 * lane + p + kHaloMax) >> 1)];
+    const float bxc = ctr.x, byc = ctr.y, bzc = ctr.z, Ic = ctr.w;
+    const int nt = ph + 1;
+    const int cbase = lane + ((kHaloMax - ph) >> 1);
+    const int rbase = ty + kHaloMax - ph;
+
+    // hypothesis-independent part of the window: bilateral weights
+    // w = exp(-(I - I_c)^2 / (2 sigma_c^2) - (dx^2 + dy^2) / (2 sigma_x^2)) (PatchMatchCuda.cu:148-149)
+    float sw = 0.f, swx = 0.f, swxx = 0.f;
+    for (int m1 = 0; m1 < nt; ++m1) {
+        for (int m2 = 0; m2 < nt; ++m2) {
+            const float4 e = tile[(rbase + 2 * m1) * kTileCols + cbase + m2];
+            const float xs = e.w - Ic;
+            const int k1 = 2 * m1 - ph, k2 = 2 * m2 - ph;
+            const float w = expf(-xs * xs * a.color_factor - (float)(k2 * k2 + k1 * k1) * a.dist_factor);
+            wsm[(m1 * nt + m2) * kThreads + tid] = w;
+            sw += w;
+            swx = fmaf(w, xs, swx);
+            swxx = fmaf(w * xs, xs, swxx);
+        }
+    }
+
+    const size_t idx = (size_t)i * W + j;
+    const float4 cur = a.plane[idx];
+    float score = a.score[idx];
+    int best = a.best[idx];
+    float hx = cur.x, hy = cur.y, hz = cur.z;   // plane_*_hyp of the reference
+    const float curr_depth = cur.w;
+    float cx = hx, cy = hy, cz = hz, current_depth = curr_depth;
+    float depth_hyp = 0.f;
+    const float shift = Img::shift_for(Ic);
+    const float halfW = 0.5f * a.Wf, halfH = 0.5f * a.Hf;
+    const int nh = a.mode == kModeScore ? 1 : 14;
+
+#pragma unroll 1
+    for (int h = 0; h < nh; ++h) {
+        float px, py, pz;
+        if (a.mode == kModeScore) {
+            px = hx; py = hy; pz = hz;
+        } else if (h < 8) {
+            // neighbours (0,1),(1,0),(0,-1),(-1,0),(0,3),(3,0),(0,-3),(-3,0) (PatchMatchCuda.cu:305)
+            const int sel = h & 3, far = (h >> 2) ? 3 : 1;
+            const int di = (sel == 1) ? far : (sel == 3 ? -far : 0);
+            const int dj = (sel == 0) ? far : (sel == 2 ? -far : 0);
+            const float4 np = a.plane[(size_t)(i + di) * W + (j + dj)];
+            px = np.x; py = np.y; pz = np.z;
+        } else {
+            const int t = h - 8;
+            if (t == 0) {
+                // current depth after propagation (PatchMatchCuda.cu:340-341)
+                const float dn = __fadd_rn(__fadd_rn(__fmul_rn(bxc, hx), __fmul_rn(byc, hy)), __fmul_rn(bzc, hz));
+                current_depth = __fdiv_rn(1.0f, fmaxf(1e-6f, fabsf(dn)));
+                cx = hx; cy = hy; cz = hz;
+                // 18 standard normals of this visit: Philox tag sweep + 1
+                // block d gives pairs 2d, 2d+1 = normals 4d .. 4d+3 (18 used)
+                const uint32_t pix = (uint32_t)idx;
+#pragma unroll 1
+                for (int d = 0; d < 5; ++d) {
+                    const uint4 q = philox_block(a.seed, a.keyframe, pix, (uint32_t)(a.sweep + 1), (uint32_t)d);
+                    const float2 z0 = box_muller(q.x, q.y);
+                    nsm[(4 * d) * kThreads + tid] = z0.x;
+                    nsm[(4 * d + 1) * kThreads + tid] = z0.y;
+                    if (d < 4) {
+                        const float2 z1 = box_muller(q.z, q.w);
+                        nsm[(4 * d + 2) * kThreads + tid] = z1.x;
+                        nsm[(4 * d + 3) * kThreads + tid] = z1.y;
+                    }
+                }
+            }
+            // refinement t (PatchMatchCuda.cu:364-382)
+            const float ra = nsm[(3 * t) * kThreads + tid];
+            const float rb = nsm[(3 * t + 1) * kThreads + tid];
+            const float rc = nsm[(3 * t + 2) * kThreads + tid];
+            depth_hyp = __fmul_rn(current_depth, expf(__fmul_rn(a.depth_range[t], ra)));
+            const float nr = a.normal_range[t];
+            const float nhx = __fadd_rn(cx, __fmul_rn(nr, ra));
+            const float nhy = __fadd_rn(cy, __fmul_rn(nr, rb));
+            const float nhz = __fadd_rn(cz, __fmul_rn(nr, rc));
+            const float qx = __fmul_rn(depth_hyp, bxc), qy = __fmul_rn(depth_hyp, byc), qz = __fmul_rn(depth_hyp, bzc);
+            const float den = __fadd_rn(__fadd_rn(__fmul_rn(nhx, qx), __fmul_rn(nhy, qy)), __fmul_rn(nhz, qz));
+            px = __fdiv_rn(nhx, den); py = __fdiv_rn(nhy, den); pz = __fdiv_rn(nhz, den);
+        }
+
+        // ---- cost of hypothesis (px, py, pz) ----
+        TapAccum<S, Img> acc;
+        acc.zero();
+#pragma unroll 1
+        for (int m1 = 0; m1 < nt; ++m1) {
+            const float4 *trow = tile + (rbase + 2 * m1) * kTileCols + cbase;
+            const float *wrow = wsm + (m1 * nt) * kThreads + tid;
+#pragma unroll 1
+            for (int m2 = 0; m2 < nt; ++m2) {
+                const float4 e = trow[m2];
+                const float w = wrow[m2 * kThreads];
+                acc.add(a.P, a.quad, a.qpitch, a.Wf, a.Hf, halfW, halfH, shift, px, py, pz, e.x, e.y, e.z, w,
+                        e.w - Ic);
+            }
+        }
+        float ncc[S];
+#pragma unroll
+        for (int r = 0; r < S; ++r) ncc[r] = ncc_from_moments(sw, swx, swxx, acc.swy[r], acc.swyy[r], acc.swxy[r]);
+        int hb;
+        float sc = combine_scores<S>(ncc, a.combine, a.top_k, &hb);
+
+        if (a.mode == kModeScore) {
+            score = sc;
+            best = hb;
+        } else if (h < 8) {
+            // smoothness weighting of propagated planes (PatchMatchCuda.cu:322-337)
+            const float scale = __fadd_rn(__fadd_rn(__fmul_rn(px, bxc), __fmul_rn(py, byc)), __fmul_rn(pz, bzc));
+            const float denom = __fdiv_rn(1.0f, fmaxf(1e-6f, fabsf(scale)));
+            const float dq = __fdiv_rn(__fsub_rn(curr_depth, denom), curr_depth);
+            const float dsf = expf(__fmul_rn(-__fmul_rn(dq, dq), 1250.0f));
+            const float prod = __fadd_rn(__fadd_rn(__fmul_rn(hx, px), __fmul_rn(hy, py)), __fmul_rn(hz, pz));
+            const float ex = __fsub_rn(hx, px), ey = __fsub_rn(hy, py), ez = __fsub_rn(hz, pz);
+            const float nrm = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey)), __fmul_rn(ez, ez)));
+            const float ac = acosf(__fdiv_rn(prod, nrm));
+            const float psf = expf(__fmul_rn(-__fmul_rn(ac, ac), 8.0f));
+            sc = __fmul_rn(sc, __fmul_rn(__fsub_rn(1.0f, dsf), __fsub_rn(1.0f, psf)));
+            if (sc > score) { hx = px; hy = py; hz = pz; score = sc; best = hb; }
+        } else {
+            if (sc > score) { cx = px; cy = py; cz = pz; score = sc; current_depth = depth_hyp; best = hb; }
+        }
+    }
+
+    a.score[idx] = score;
+    a.best[idx] = (int8_t)best;
+    if (a.mode == kModeSweep) {
+        const float den = __fadd_rn(__fadd_rn(__fmul_rn(bxc, cx), __fmul_rn(byc, cy)), __fmul_rn(bzc, cz));
+        a.plane[idx] = make_float4(cx, cy, cz, __fdiv_rn(1.0f, fmaxf(1e-6f, fabsf(den))));
+    }
+}
+
+// Fixed-hypothesis scoring: one thread per (pixel, plane); taps read straight
+// from global memory (L1-resident) instead of a staged tile.  Same per-tap
+// arithmetic (TapAccum) as the tile kernel.
+template <int S, class Img>
+__global__ void __launch_bounds__(256) hyp_kernel(const __grid_constant__ HypArgs a) {
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= a.n) return;
+    const int2 ij = a.ij[h];
+    const int i = ij.x, j = ij.y, W = a.W, ph = a.patch_half;
+    const float Ic = a.ref[(size_t)i * W + j];
+    const float px = a.planes[3 * h], py = a.planes[3 * h + 1], pz = a.planes[3 * h + 2];
+    const float shift = Img::shift_for(Ic);
+    const float halfW = 0.5f * a.Wf, halfH = 0.5f * a.Hf;
+    float sw = 0.f, swx = 0.f, swxx = 0.f;
+    TapAccum<S, Img> acc;
+    acc.zero();
+    for (int k1 = -ph; k1 <= ph; k1 += 2) {
+        const int R = i + k1;
+        const float2 rt = a.row_trig[R];
+        for (int k2 = -ph; k2 <= ph; k2 += 2) {
+            const int C = j + k2;
+            const float2 ct = a.col_trig[C];
+            const float x = a.ref[(size_t)R * W + C];
+            const float xs = x - Ic;
+            const float w = expf(-xs * xs * a.color_factor - (float)(k2 * k2 + k1 * k1) * a.dist_factor);
+            sw += w;
+            swx = fmaf(w, xs, swx);
+            swxx = fmaf(w * xs, xs, swxx);
+            acc.add(a.P, a.quad, a.qpitch, a.Wf, a.Hf, halfW, halfH, shift, px, py, pz, rt.x * ct.x, -rt.y,
+                    rt.x * ct.y, w, xs);
+        }
+    }
+    float ncc[S];
+#pragma unroll
+    for (int r = 0; r < S; ++r) {
+        ncc[r] = ncc_from_moments(sw, swx, swxx, acc.swy[r], acc.swyy[r], acc.swxy[r]);
+        if (a.per_source) a.per_source[(size_t)h * S + r] = ncc[r];
+    }
+    int hb;
+    const float sc = combine_scores<S>(ncc, a.combine, a.top_k, &hb);
+    if (a.scores) a.scores[h] = sc;
+    if (a.best) a.best[h] = hb;
+}
+
+}  // namespace pm

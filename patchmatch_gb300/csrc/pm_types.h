@@ -1,0 +1,67 @@
+// Internal types shared by the host code and the kernels.
+#pragma once
+
+#include <stdint.h>
+
+#include "pm_gb300.h"
+
+namespace pm {
+
+constexpr int kMaxSrc = PM_MAX_SOURCES;
+
+// Composed reference-camera -> source-camera poses, FP64-composed on the
+// host and rounded to float: X_r = M_r X_c + c_r.
+struct PmPoses {
+    float M[kMaxSrc][9];
+    float c[kMaxSrc][3];
+};
+
+// Kernel arguments of the tile kernels (init scoring and red-black sweeps).
+struct SweepArgs {
+    PmPoses P;
+    const void *quad[kMaxSrc];  // per-source quad-packed sampling images
+    int qpitch;                 // quads per row (W + 1)
+    const float2 *row_trig;     // H entries: (cos lat, sin lat)
+    const float2 *col_trig;     // W entries: (sin lon, cos lon)
+    const float *ref;           // H x W reference intensities (float)
+    float4 *plane;              // H x W: plane (x, y, z) and depth (w)
+    float *score;               // H x W
+    int8_t *best;               // H x W
+    int W, H;
+    float Wf, Hf;
+    int patch_half;
+    int colour;                 // 0 = red, 1 = black: pixels with (i + j + colour) even
+    int sweep;                  // sweep index (Philox tag = sweep + 1)
+    int mode;                   // 0 = score own plane, 1 = red-black update
+    int combine, top_k;
+    uint32_t seed, keyframe;
+    float color_factor;         // 1 / (2 sigma_color^2)
+    float dist_factor;          // 1 / (2 sigma_x^2)
+    float depth_range[6];       // refinement depth ranges 0.02 * 0.3^t (float, reference rounding)
+    float normal_range[6];      // refinement normal ranges 0.5 * 0.8^t
+};
+
+enum { kModeScore = 0, kModeSweep = 1 };
+
+// Arguments of the fixed-hypothesis scoring kernel.
+struct HypArgs {
+    PmPoses P;
+    const void *quad[kMaxSrc];
+    int qpitch;
+    const float2 *row_trig;
+    const float2 *col_trig;
+    const float *ref;
+    int W, H;
+    float Wf, Hf;
+    int patch_half;
+    int combine, top_k;
+    float color_factor, dist_factor;
+    int n;
+    const int2 *ij;
+    const float *planes;  // n x 3
+    float *scores;        // n
+    int *best;            // n
+    float *per_source;    // n x S or null
+};
+
+}  // namespace pm

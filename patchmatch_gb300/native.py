@@ -1,0 +1,317 @@
+"""ctypes binding of the densifier's C ABI (``include/pm_gb300.h``).
+
+Everything here calls straight into ``libpm_gb300.so``; there is no Python or
+CPU implementation of the densifier to fall back to.  Arrays are numpy (host)
+buffers unless a raw pointer (int) is passed.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._native import load_pm_lib
+
+PM_OK, PM_EINVAL, PM_ENOMEM, PM_EBUDGET, PM_ETIMEOUT, PM_ECUDA, PM_ENOTREADY, PM_ECANCELLED, PM_ENOTBUILT = range(9)
+COMBINE_FOLD, COMBINE_MAX, COMBINE_TOPK = 0, 1, 2
+SEAM_CLAMP, SEAM_WRAP = 0, 1
+INIT_LOGUNIFORM_HEMI, INIT_REF_UNIFORM = 0, 1
+IMAGE_U8, IMAGE_F16 = 0, 1
+MAX_SOURCES = 10
+
+# Every exported symbol declared in include/pm_gb300.h.
+EXPORTS = (
+    "pm_params_default", "pm_create", "pm_destroy", "pm_last_error", "pm_status_string", "pm_launch_count",
+    "pm_densify", "pm_request_create", "pm_request_destroy", "pm_request_bytes", "pm_request_set_params",
+    "pm_request_set_view", "pm_request_init", "pm_request_set_state", "pm_request_sweep", "pm_request_postprocess",
+    "pm_request_run", "pm_request_read", "pm_request_synchronize", "pm_request_depth_device",
+    "pm_score_hypotheses", "pm_filter_consistency", "pm_fuse",
+)
+
+
+class Params(C.Structure):
+    _fields_ = [("patch_half", C.c_int), ("iterations", C.c_int), ("combine", C.c_int), ("top_k", C.c_int),
+                ("seam", C.c_int), ("init_mode", C.c_int), ("image_format", C.c_int), ("postprocess", C.c_int),
+                ("min_depth", C.c_float), ("max_depth", C.c_float), ("min_score", C.c_float),
+                ("min_patch_sd", C.c_float), ("sigma_color", C.c_float), ("sigma_x", C.c_float),
+                ("seed", C.c_uint32), ("keyframe_id", C.c_uint32)]
+
+
+class View(C.Structure):
+    _fields_ = [("gray", C.c_void_p), ("pitch_bytes", C.c_size_t), ("mask", C.c_void_p),
+                ("R_cw", C.c_double * 9), ("t_cw", C.c_double * 3)]
+
+
+class Maps(C.Structure):
+    _fields_ = [("depth", C.c_void_p), ("score", C.c_void_p), ("plane", C.c_void_p), ("normal", C.c_void_p),
+                ("best_view", C.c_void_p)]
+
+
+class Points(C.Structure):
+    _fields_ = [("capacity", C.c_int), ("count", C.c_int), ("xyz", C.c_void_p), ("bgr", C.c_void_p),
+                ("ij", C.c_void_p)]
+
+
+_vp, _sz = C.c_void_p, C.c_size_t
+
+
+def lib():
+    L = load_pm_lib()
+    if getattr(L, "_pm_typed", False):
+        return L
+    L.pm_params_default.argtypes = [C.POINTER(Params)]
+    L.pm_create.argtypes = [C.c_int, _sz, C.POINTER(_vp)]
+    L.pm_destroy.argtypes = [_vp]
+    L.pm_last_error.restype = C.c_char_p
+    L.pm_last_error.argtypes = [_vp]
+    L.pm_status_string.restype = C.c_char_p
+    L.pm_status_string.argtypes = [C.c_int]
+    L.pm_launch_count.restype = C.c_uint64
+    L.pm_launch_count.argtypes = [_vp]
+    L.pm_densify.argtypes = [_vp, C.c_int, C.c_int, C.POINTER(View), C.c_int, C.POINTER(Params), C.POINTER(Maps)]
+    L.pm_request_create.argtypes = [_vp, C.c_int, C.c_int, C.c_int, C.POINTER(Params), C.POINTER(_vp)]
+    L.pm_request_destroy.argtypes = [_vp]
+    L.pm_request_bytes.restype = _sz
+    L.pm_request_bytes.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int]
+    L.pm_request_set_params.argtypes = [_vp, C.POINTER(Params)]
+    L.pm_request_set_view.argtypes = [_vp, C.c_int, C.POINTER(View)]
+    L.pm_request_init.argtypes = [_vp]
+    L.pm_request_set_state.argtypes = [_vp, _vp, _vp]
+    L.pm_request_sweep.argtypes = [_vp, C.c_int, C.c_int]
+    L.pm_request_postprocess.argtypes = [_vp]
+    L.pm_request_run.argtypes = [_vp]
+    L.pm_request_read.argtypes = [_vp, C.POINTER(Maps), C.c_int]
+    L.pm_request_synchronize.argtypes = [_vp]
+    L.pm_request_depth_device.restype = _vp
+    L.pm_request_depth_device.argtypes = [_vp]
+    L.pm_score_hypotheses.argtypes = [_vp, C.c_int, _vp, _vp, _vp, _vp, _vp]
+    L.pm_filter_consistency.argtypes = [_vp, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, C.c_int, C.c_float,
+                                        C.c_int, C.c_float, _vp]
+    L.pm_fuse.argtypes = [_vp, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, C.c_float, _vp, C.POINTER(Points)]
+    L._pm_typed = True
+    return L
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    if isinstance(a, int):
+        return a
+    if isinstance(a, np.ndarray):
+        assert a.flags["C_CONTIGUOUS"], "array must be C-contiguous"
+        return a.ctypes.data
+    if hasattr(a, "data_ptr"):  # torch tensor
+        return a.data_ptr()
+    raise TypeError(type(a))
+
+
+class PmError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"[{status}] {msg}")
+        self.status = status
+
+
+def default_params(**kw) -> Params:
+    p = Params()
+    lib().pm_params_default(C.byref(p))
+    for k, v in kw.items():
+        if not hasattr(p, k):
+            raise AttributeError(k)
+        setattr(p, k, v)
+    return p
+
+
+def make_view(gray, R, t, mask=None, pitch_bytes: int = 0) -> View:
+    v = View()
+    v.gray = _ptr(gray)
+    v.pitch_bytes = pitch_bytes
+    v.mask = _ptr(mask)
+    R = np.asarray(R, np.float64).reshape(9)
+    t = np.asarray(t, np.float64).reshape(3)
+    for a in range(9):
+        v.R_cw[a] = R[a]
+    for a in range(3):
+        v.t_cw[a] = t[a]
+    return v
+
+
+class Context:
+    """One CUDA stream + device buffers on one GPU (pm_ctx)."""
+
+    def __init__(self, device: int = 0, hbm_budget: int = 0):
+        self._L = lib()
+        h = C.c_void_p()
+        rc = self._L.pm_create(device, hbm_budget, C.byref(h))
+        if rc != PM_OK:
+            raise PmError(rc, f"pm_create failed: {self._L.pm_status_string(rc).decode()}")
+        self.h = h.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._L.pm_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def check(self, rc: int):
+        if rc != PM_OK:
+            raise PmError(rc, self._L.pm_last_error(self.h).decode())
+
+    @property
+    def launches(self) -> int:
+        return int(self._L.pm_launch_count(self.h))
+
+    def last_error(self) -> str:
+        return self._L.pm_last_error(self.h).decode()
+
+    # ---- one-shot ----
+    def densify(self, images, R, t, params: Params | None = None, mask=None, want=("depth", "score", "normal")):
+        """images: list of (H, W) uint8 / float16 arrays, view 0 = reference."""
+        params = params or default_params()
+        H, W = images[0].shape
+        views = (View * len(images))(*[make_view(np.ascontiguousarray(im), R[k], t[k], mask if k == 0 else None)
+                                       for k, im in enumerate(images)])
+        out, maps = _alloc_maps(H, W, want)
+        self.check(self._L.pm_densify(self.h, W, H, views, len(images), C.byref(params), C.byref(maps)))
+        return out
+
+    def request(self, W: int, H: int, n_sources: int, params: Params | None = None) -> "Request":
+        return Request(self, W, H, n_sources, params or default_params())
+
+    # ---- filter / fuse ----
+    def filter_consistency(self, depths, R, t, center: int, thr: float, min_consistent: int = 3,
+                           reproj_px: float = 0.0):
+        depths = [np.ascontiguousarray(d, np.float32) for d in depths]
+        H, W = depths[0].shape
+        arr = (C.c_void_p * len(depths))(*[d.ctypes.data for d in depths])
+        R = np.ascontiguousarray(R, np.float64)
+        t = np.ascontiguousarray(t, np.float64)
+        out = np.zeros((H, W), np.float32)
+        self.check(self._L.pm_filter_consistency(self.h, W, H, len(depths), C.cast(arr, C.c_void_p), _ptr(R),
+                                                 _ptr(t), center, thr, min_consistent, reproj_px, _ptr(out)))
+        return out
+
+    def fuse(self, depths, R, t, bgr, thr: float):
+        """Returns (pruned, xyz[n,3] f64, bgr[n,3] u8, ij[n,2] i32, mutated depths)."""
+        depths = [np.ascontiguousarray(d, np.float32).copy() for d in depths]
+        H, W = depths[0].shape
+        arr = (C.c_void_p * len(depths))(*[d.ctypes.data for d in depths])
+        R = np.ascontiguousarray(R, np.float64)
+        t = np.ascontiguousarray(t, np.float64)
+        pruned = np.zeros((H, W), np.float32)
+        cap = H * W
+        xyz = np.zeros((cap, 3), np.float64)
+        cols = np.zeros((cap, 3), np.uint8)
+        ij = np.zeros((cap, 2), np.int32)
+        pts = Points(cap, 0, xyz.ctypes.data, cols.ctypes.data, ij.ctypes.data)
+        bgr = None if bgr is None else np.ascontiguousarray(bgr, np.uint8)
+        self.check(self._L.pm_fuse(self.h, W, H, len(depths), C.cast(arr, C.c_void_p), _ptr(R), _ptr(t), _ptr(bgr),
+                                   thr, _ptr(pruned), C.byref(pts)))
+        n = pts.count
+        return pruned, xyz[:n], cols[:n], ij[:n], depths
+
+
+def _alloc_maps(H, W, want):
+    out = {}
+    maps = Maps()
+    for name in want:
+        if name in ("depth", "score"):
+            a = np.zeros((H, W), np.float32)
+        elif name in ("plane", "normal"):
+            a = np.zeros((H, W, 3), np.float32)
+        elif name == "best_view":
+            a = np.zeros((H, W), np.int32)
+        else:
+            raise KeyError(name)
+        out[name] = a
+        setattr(maps, name, a.ctypes.data)
+    if "depth" not in out:
+        a = np.zeros((H, W), np.float32)
+        out["depth"] = a
+        maps.depth = a.ctypes.data
+    return out, maps
+
+
+class Request:
+    """Device-resident state of one keyframe (pm_request)."""
+
+    def __init__(self, ctx: Context, W: int, H: int, n_sources: int, params: Params):
+        self.ctx, self.W, self.H, self.S = ctx, W, H, n_sources
+        self._L = ctx._L
+        self.params = params
+        h = C.c_void_p()
+        ctx.check(self._L.pm_request_create(ctx.h, W, H, n_sources, C.byref(params), C.byref(h)))
+        self.h = h.value
+        self._keep = {}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._L.pm_request_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_params(self, params: Params):
+        self.params = params
+        self.ctx.check(self._L.pm_request_set_params(self.h, C.byref(params)))
+
+    def set_view(self, k: int, gray, R, t, mask=None, pitch_bytes: int = 0):
+        if isinstance(gray, np.ndarray):
+            gray = np.ascontiguousarray(gray)
+            self._keep[k] = (gray, mask)
+        v = make_view(gray, R, t, mask, pitch_bytes)
+        self.ctx.check(self._L.pm_request_set_view(self.h, k, C.byref(v)))
+
+    def set_views(self, images, R, t, mask=None):
+        for k, im in enumerate(images):
+            self.set_view(k, im, R[k], t[k], mask if k == 0 else None)
+
+    def init(self):
+        self.ctx.check(self._L.pm_request_init(self.h))
+
+    def set_state(self, planes, scores=None):
+        planes = np.ascontiguousarray(planes, np.float32)
+        scores = None if scores is None else np.ascontiguousarray(scores, np.float32)
+        self.ctx.check(self._L.pm_request_set_state(self.h, _ptr(planes), _ptr(scores)))
+
+    def sweep(self, first_half: int, n_half: int):
+        self.ctx.check(self._L.pm_request_sweep(self.h, first_half, n_half))
+
+    def postprocess(self):
+        self.ctx.check(self._L.pm_request_postprocess(self.h))
+
+    def run(self):
+        self.ctx.check(self._L.pm_request_run(self.h))
+
+    def synchronize(self):
+        self.ctx.check(self._L.pm_request_synchronize(self.h))
+
+    def read(self, raw: bool = False, want=("depth", "score", "plane", "normal", "best_view")):
+        out, maps = _alloc_maps(self.H, self.W, want)
+        self.ctx.check(self._L.pm_request_read(self.h, C.byref(maps), 1 if raw else 0))
+        return out
+
+    def score_hypotheses(self, ij, planes, per_source: bool = False):
+        ij = np.ascontiguousarray(ij, np.int32)
+        planes = np.ascontiguousarray(planes, np.float32)
+        n = ij.shape[0]
+        scores = np.zeros(n, np.float32)
+        best = np.zeros(n, np.int32)
+        ps = np.zeros((n, self.S), np.float32) if per_source else None
+        self.ctx.check(self._L.pm_score_hypotheses(self.h, n, _ptr(ij), _ptr(planes), _ptr(scores), _ptr(best),
+                                                   _ptr(ps)))
+        return (scores, best, ps) if per_source else (scores, best)
