@@ -1,0 +1,325 @@
+"""Benchmark of the GB300 densifier on the 1920x960, 6-source workload.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+A step densifies one keyframe: Philox initialisation, init scoring, 8
+red-black sweeps (propagation + 6 refinements per pixel visit) and the
+post-filter.  The metric is Mpix*views/s = (W*H/1e6) * sources / seconds per
+keyframe (whole job: summed over GPUs; N > 1 runs independent replicas).
+
+  value : device-resident inputs, CUDA-event time of the step on the
+          context's stream; L2 is flushed (256 MB write) between steps.
+  e2e   : the same step through the public C ABI (pm_densify) from pinned
+          host buffers: host->device copy of the 7 images and device->host
+          copy of the depth and score maps are inside the timed region.
+
+--impl reference times the reference's per-pixel CPU algorithm (the oracle's
+restatement of the reference kernel arithmetic, OpenMP on all host cores) on
+a bounded band of rows of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+W, H, S, SWEEPS = 1920, 960, 6, 8
+METRIC = "Mpix·views/s and p50/p99 keyframe latency, served vs plain at ≤1% depth error"
+UNIT = "Mpix·views/s"
+WORKLOAD = ("plain PatchMatch, one 1920x960 u8 equirect keyframe + 6 sources per step, 8 red-black sweeps, "
+            "11x11 window at stride 2, fold view combination, room + 5 boxes + cylinder scene")
+FLOP_PER_SAMPLE = 40  # algorithmic FP32 work of one (pixel, hypothesis, source, tap) sample
+
+
+def _mpix_views(ms: float) -> float:
+    return (W * H / 1e6) * S / (ms / 1e3)
+
+
+def _samples_per_half_sweep() -> float:
+    ph = 5
+    interior = (W - 2 * (ph + 1) + 1) * (H - 2 * (ph + 1) + 1)
+    return interior / 2 * 14 * S * 36
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is None:
+            return
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        self.lines = [ln for ln in out.splitlines() if ln.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() in ("active", "1"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, 0, None
+    import torch.distributed as dist
+    rank = int(os.environ["RANK"])
+    local = int(os.environ.get("LOCAL_RANK", rank))
+    dist.init_process_group("gloo")  # barriers and the max-reduction only; replicas share nothing
+    return rank, ws, local, dist
+
+
+def _barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def _allmax(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _traffic_from_profile():
+    """DRAM bytes per sweep launch from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "tile_kernel_1920x960x6.md")
+    if not os.path.exists(path):
+        return None
+    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", open(path).read())
+    return float(m.group(1)) if m else None
+
+
+def cpu_sample(target_s: float = 12.0, threads: int = 0):
+    """Reference per-pixel algorithm (oracle, reference float arithmetic) on a
+    band of rows of the workload, 8 sweeps; returns Mpix*views/s and the band."""
+    from oracle import oracle as O
+    from patchmatch_gb300 import scene
+    req = scene.config_request(2, seed=0)
+    V = O.Views.from_request(req)
+    cp = O.cost_params(arith=O.ARITH_F32_REF)
+    threads = threads or os.cpu_count() or 1
+    # calibrate on 4 rows x 1 sweep
+    r0 = H // 2
+    t = O.patchmatch(V, cp, iterations=1, row_lo=r0, row_hi=r0 + 4, threads=threads)["seconds"]
+    per_row_sweep = max(t / 4.0, 1e-4)
+    rows = int(max(2, min(H - 20, target_s / (per_row_sweep * SWEEPS))))
+    lo = max(6, r0 - rows // 2)
+    res = O.patchmatch(V, cp, iterations=SWEEPS, row_lo=lo, row_hi=lo + rows, threads=threads)
+    secs = res["seconds"]
+    value = (W * rows / 1e6) * S / secs
+    return value, rows, secs, threads, V, req
+
+
+def run_reference(args):
+    rank, ws, _, dist = _dist()
+    if rank != 0:
+        return
+    steps = []
+    info = None
+    for k in range(args.warmup + args.steps):
+        v, rows, secs, threads, _, _ = cpu_sample(target_s=args.cpu_seconds)
+        if k >= args.warmup:
+            steps.append((v, secs))
+        info = (rows, threads)
+    value = statistics.median(v for v, _ in steps)
+    rows, threads = info
+    sample = f"rows {H // 2 - rows // 2}..+{rows} of the 1920x960x6 workload, all {SWEEPS} sweeps"
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * statistics.median(s for _, s in steps),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "W": W, "H": H, "sources": S, "sweeps": SWEEPS,
+                       "sample": sample},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    import torch
+    rank, ws, local, dist = _dist()
+    torch.cuda.set_device(local)
+    from patchmatch_gb300 import native, scene
+
+    req = scene.config_request(2, seed=rank)
+    imgs = [np.ascontiguousarray(v.gray_u8) for v in req.views]
+    ctx = native.Context(local)
+    p = native.default_params(iterations=SWEEPS, seed=rank)
+    r = ctx.request(W, H, S, p)
+    r.set_views(imgs, req.R, req.t)
+    stream = torch.cuda.ExternalStream(ctx.stream_handle)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+
+    # --- device-resident steps ---
+    for _ in range(args.warmup):
+        r.run()
+    r.synchronize()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    launches0 = ctx.launches
+    _barrier(dist)
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter()
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(k & 0xFF)  # L2 flush between steps, outside the events
+                ev[k][0].record(stream)
+            r.run()
+            with torch.cuda.stream(stream):
+                ev[k][1].record(stream)
+        r.synchronize()
+        torch.cuda.synchronize()
+    wall = time.perf_counter() - t_wall
+    _barrier(dist)
+    gpu_launches = ctx.launches - launches0
+    ms = [a.elapsed_time(b) for a, b in ev]
+    ms_step = _allmax(dist, sum(ms) / len(ms))
+    value = ws * _mpix_views(ms_step)
+    lat = np.array(ms)
+
+    # --- dominant kernel: one red-black half-sweep, timed on the context stream ---
+    r.run()
+    nhalf = 2 * SWEEPS
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+    r.sweep(0, nhalf)
+    with torch.cuda.stream(stream):
+        e1.record(stream)
+    r.synchronize()
+    sweep_ms = e0.elapsed_time(e1) / nhalf
+    achieved = FLOP_PER_SAMPLE * _samples_per_half_sweep() / (sweep_ms * 1e-3) / 1e12
+    peak = ctx.probe_fp32_peak()
+
+    # --- end to end through the C ABI from pinned host buffers ---
+    pin = [torch.from_numpy(im).pin_memory() for im in imgs]
+    d_out = torch.empty((H, W), dtype=torch.float32).pin_memory()
+    s_out = torch.empty((H, W), dtype=torch.float32).pin_memory()
+    import ctypes as C
+    views = (native.View * (S + 1))(*[native.make_view(pin[k].data_ptr(), req.R[k], req.t[k]) for k in range(S + 1)])
+    maps = native.Maps()
+    maps.depth = d_out.data_ptr()
+    maps.score = s_out.data_ptr()
+    L = native.lib()
+    for _ in range(max(1, args.warmup)):
+        ctx.check(L.pm_densify(ctx.h, W, H, views, S + 1, C.byref(p), C.byref(maps)))
+    _barrier(dist)
+    e2e_t = []
+    for _ in range(args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.check(L.pm_densify(ctx.h, W, H, views, S + 1, C.byref(p), C.byref(maps)))
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_ms = _allmax(dist, 1e3 * sum(e2e_t) / len(e2e_t))
+    e2e_value = ws * _mpix_views(e2e_ms)
+    valid = float((d_out.numpy() > 0).mean())
+    gt = req.views[0].depth
+    dn = d_out.numpy()
+    m = dn > 0
+    acc = float((np.abs(dn[m] - gt[m]) / gt[m] < 0.01).mean()) if m.any() else 0.0
+
+    traffic = _traffic_from_profile()
+    line = None
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu:
+            v, rows, secs, threads, _, _ = cpu_sample(target_s=args.cpu_seconds)
+            cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                   "sample": f"{rows} rows x 1920 of the same workload, all {SWEEPS} sweeps, "
+                             f"{secs:.1f} s, reference float arithmetic (oracle), OpenMP"}
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded ray-cast scene, analytic ground truth)",
+            "config": {"workload": WORKLOAD, "W": W, "H": H, "sources": S, "sweeps": SWEEPS, "image": "u8",
+                       "parallelism": "replicas" if ws > 1 else "single GPU",
+                       "l2": "flushed between steps (256 MB write outside the timed events)"},
+            "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                           "form": "plain (one keyframe at a time)"},
+            "quality": {"valid_fraction": valid, "within_1pct_of_truth": acc},
+            "e2e": {"value": e2e_value, "unit": UNIT, "ms_per_step": e2e_ms,
+                    "h2d_bytes_per_step": int((S + 1) * W * H), "d2h_bytes_per_step": int(2 * 4 * W * H)},
+            "roofline": {"bound": "fp32", "kernel": "tile_kernel (red-black half-sweep)",
+                         "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                         "peak_source": "in-run FFMA probe (pm_probe_fp32_peak); MEASURED_PEAKS.json has no FP32 figure",
+                         "flop_per_sample": FLOP_PER_SAMPLE, "samples_per_launch": _samples_per_half_sweep(),
+                         "launch_ms": sweep_ms, "traffic": traffic},
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "gpu_launches": int(gpu_launches),
+            "wall_s_timed_region": wall,
+        }
+        print(json.dumps(line))
+    r.close()
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

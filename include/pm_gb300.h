@@ -117,6 +117,12 @@ const char *pm_last_error(const pm_ctx *ctx);
 const char *pm_status_string(int status);
 /* Kernel launches issued by this context so far (instrumentation). */
 uint64_t pm_launch_count(const pm_ctx *ctx);
+/* The context's CUDA stream (a cudaStream_t), for timing with CUDA events. */
+void *pm_stream(const pm_ctx *ctx);
+/* Measured FP32 FMA throughput of this GPU in TFLOP/s (an FFMA-bound probe
+ * kernel on the context's stream; 1 FMA = 2 flop).  The densifier's cost
+ * kernel is bounded by the FP32 pipe, so this is its roofline denominator. */
+int pm_probe_fp32_peak(pm_ctx *ctx, double *tflops);
 
 /* One keyframe, host buffers in and out (synchronous).  views[0] is the
  * reference keyframe, views[1..n_views-1] its sources (1..PM_MAX_SOURCES).

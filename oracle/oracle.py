@@ -67,6 +67,7 @@ def lib():
         L.or_philox4x32_10.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
         L.or_refine_normals.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, _fp]
         L.or_bearing64.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _dp]
+        L.or_bearing_ref_f32.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _fp]
         L.or_cost.restype = C.c_double
         L.or_cost.argtypes = [C.POINTER(ORViews), C.POINTER(ORCostParams), C.c_int, C.c_int, _dp, _dp,
                               C.POINTER(C.c_int)]
@@ -227,6 +228,12 @@ def bearing64(W, H, i, j):
     b = (C.c_double * 3)()
     lib().or_bearing64(W, H, i, j, b)
     return np.array(list(b))
+
+
+def bearing_ref_f32(W, H, i, j):
+    b = (C.c_float * 3)()
+    lib().or_bearing_ref_f32(W, H, i, j, b)
+    return np.array(list(b), np.float32)
 
 
 def gt_plane(depth, normal, W, H, i, j):

@@ -93,6 +93,8 @@ static void bearing_ref_f32(int W, int H, int i, int j, float b[3])
     b[0] = bx * nrm; b[1] = by * nrm; b[2] = bz * nrm;
 }
 
+void or_bearing_ref_f32(int W, int H, int i, int j, float b[3]) { bearing_ref_f32(W, H, i, j, b); }
+
 /* The reference host's double bearing table (depthmap.cc:113-128,1213-1223):
  * float trig, promoted to double, normalised in double. */
 static void bearing_ref_host(int W, int H, int i, int j, double b[3])
@@ -501,7 +503,7 @@ double or_patchmatch(const or_views *v, const or_run_params *rp, float *plane, f
         }
 #ifdef _OPENMP
     double t0 = omp_get_wtime();
-#pragma omp parallel for schedule(dynamic, 1)
+#pragma omp parallel for collapse(2) schedule(dynamic, 128)
 #endif
     for (int i = lo; i < hi; ++i)
         for (int j = 0; j < W; ++j) {
@@ -514,7 +516,7 @@ double or_patchmatch(const or_views *v, const or_run_params *rp, float *plane, f
     for (int s = 0; s < rp->iterations; ++s) {
         for (int off = 0; off < 2; ++off) {
 #ifdef _OPENMP
-#pragma omp parallel for schedule(dynamic, 1)
+#pragma omp parallel for collapse(2) schedule(dynamic, 128)
 #endif
             for (int i = lo; i < hi; ++i)
                 for (int j = 0; j < W; ++j) {
@@ -542,7 +544,7 @@ void or_sweeps(const or_views *v, const or_run_params *rp, float *plane, float *
     for (int hs = first_half; hs < first_half + n_half; ++hs) {
         const int off = hs & 1, s = hs >> 1;
 #ifdef _OPENMP
-#pragma omp parallel for schedule(dynamic, 1)
+#pragma omp parallel for collapse(2) schedule(dynamic, 128)
 #endif
         for (int i = lo; i < hi; ++i)
             for (int j = 0; j < W; ++j) {

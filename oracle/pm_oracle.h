@@ -94,6 +94,9 @@ void or_refine_normals(uint32_t seed, uint32_t keyframe, uint32_t pixel, uint32_
 /* Exact (FP64) bearing of pixel (i, j): pixel-corner convention, x = j. */
 void or_bearing64(int W, int H, int i, int j, double b[3]);
 
+/* The reference kernel's float bearing (PatchMatchCuda.cu:183-208). */
+void or_bearing_ref_f32(int W, int H, int i, int j, float b[3]);
+
 /* ---- cost ---- */
 /* Cost of plane hypothesis `plane` (camera frame, plane . X = 1) at pixel
  * (i, j).  Writes per-source NCC (n_src values) if ncc != NULL and the

@@ -22,6 +22,20 @@ cudaError_t configure_tile();
 
 namespace {
 
+// FFMA-bound probe: 8 independent chains per thread, 1 FMA = 2 flop.
+__global__ void fp32_probe_kernel(float *out, int iters, float a, float b) {
+    float x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+    for (int k = 0; k < iters; ++k) {
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+            x0 = fmaf(x0, a, b); x1 = fmaf(x1, a, b); x2 = fmaf(x2, a, b); x3 = fmaf(x3, a, b);
+            x4 = fmaf(x4, a, b); x5 = fmaf(x5, a, b); x6 = fmaf(x6, a, b); x7 = fmaf(x7, a, b);
+        }
+    }
+    const float s = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+    if (s == 1.2345f) out[0] = s;  // keeps the chains alive
+}
+
 struct Trig {
     int W = 0, H = 0;
     float2 *row = nullptr, *col = nullptr;
@@ -201,6 +215,8 @@ void fill_args(pm_request *r) {
     a.keyframe = p.keyframe_id;
     a.color_factor = 1.0f / (2 * p.sigma_color * p.sigma_color);
     a.dist_factor = 1.0f / (2 * p.sigma_x * p.sigma_x);
+    a.ncf = (float)(-1.4426950408889634 * a.color_factor);
+    a.ndf = (float)(-1.4426950408889634 * a.dist_factor);
     float dr = 0.02f, nr = 0.5f;  // PatchMatchCuda.cu:348-349,393-394 (float *= double)
     for (int t = 0; t < 6; ++t) {
         a.depth_range[t] = dr;
@@ -413,6 +429,36 @@ int pm_destroy(pm_ctx *ctx) {
 const char *pm_last_error(const pm_ctx *ctx) { return ctx ? ctx->err.c_str() : "no context"; }
 
 uint64_t pm_launch_count(const pm_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+void *pm_stream(const pm_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+int pm_probe_fp32_peak(pm_ctx *ctx, double *tflops) {
+    if (!ctx || !tflops) return fail(ctx, PM_EINVAL, "NULL argument");
+    PM_CUDA(ctx, cudaSetDevice(ctx->device));
+    int sms = 0;
+    PM_CUDA(ctx, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+    int rc = ensure_scratch(ctx, 256);
+    if (rc) return rc;
+    cudaEvent_t e0, e1;
+    PM_CUDA(ctx, cudaEventCreate(&e0));
+    PM_CUDA(ctx, cudaEventCreate(&e1));
+    const int iters = 2048, threads = 256, blocks = sms * 8;
+    double best = 0.0;
+    for (int rep = 0; rep < 4; ++rep) {
+        PM_CUDA(ctx, cudaEventRecord(e0, ctx->stream));
+        fp32_probe_kernel<<<blocks, threads, 0, ctx->stream>>>((float *)ctx->scratch, iters, 0.999999f, 1e-7f);
+        PM_CUDA(ctx, cudaEventRecord(e1, ctx->stream));
+        PM_CUDA(ctx, cudaEventSynchronize(e1));
+        float ms = 0.f;
+        PM_CUDA(ctx, cudaEventElapsedTime(&ms, e0, e1));
+        const double flop = 2.0 * 8 * 16 * (double)iters * threads * blocks;
+        if (rep > 0) best = std::max(best, flop / (ms * 1e-3) / 1e12);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *tflops = best;
+    return PM_OK;
+}
 
 size_t pm_request_bytes(int W, int H, int S, int fmt) {
     const size_t N = (size_t)W * H, NQ = (size_t)(W + 1) * (H + 1);
@@ -736,6 +782,8 @@ int pm_score_hypotheses(pm_request *r, int n, const int32_t *ij, const float *pl
     a.top_k = r->prm.top_k;
     a.color_factor = r->args.color_factor;
     a.dist_factor = r->args.dist_factor;
+    a.ncf = r->args.ncf;
+    a.ndf = r->args.ndf;
     a.n = n;
     a.ij = dij;
     a.planes = dpl;

@@ -109,16 +109,27 @@ __device__ __forceinline__ float lat_halfturns(float x, float y, float z) {
 // sample is one aligned load.  Texel k sits at coordinate k, matching the
 // reference's texture reads at u + 0.5 (PatchMatchCuda.cu:146).
 // ---------------------------------------------------------------------------
+// Split a coordinate c in [0, 2^22) into a cell index k and weight a in
+// [0, 1] with c = k + a, without conversion instructions: adding
+// 2^23 - 1/2 rounds c - 1/2 to an integer in the low mantissa bits.  At odd
+// integer c this gives k = c - 1, a = 1, which samples the same texel value.
+__device__ __forceinline__ void split_coord(float c, int &k, float &a) {
+    const float m = c + 8388607.5f;
+    k = (int)(__float_as_uint(m) & 0x7FFFFFu);
+    a = c - (m - 8388608.0f);
+}
+
 struct QuadU8 {
     // shift: value subtracted from every texel, given as 2^23 + I_c so the
     // byte-to-float conversion and the centring are one subtraction.
     static __device__ __forceinline__ float shift_for(float centre) { return 8388608.0f + centre; }
     static __device__ __forceinline__ float sample(const void *base, int pitch, float u, float v, float shift) {
         // u in [0, W], v in [0, H] by construction of the angle functions
-        const float fx = floorf(u), fy = floorf(v);
-        const float ax = u - fx, ay = v - fy;
-        const int x0 = (int)fx, y0 = (int)fy;
-        const uint32_t w = __ldg(static_cast<const uint32_t *>(base) + ((size_t)y0 * pitch + x0));
+        int x0, y0;
+        float ax, ay;
+        split_coord(u, x0, ax);
+        split_coord(v, y0, ay);
+        const uint32_t w = __ldg(static_cast<const uint32_t *>(base) + (y0 * pitch + x0));
         // bytes -> floats minus the centre intensity: (2^23 + byte) - (2^23 + c)
         const float t00 = __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540)) - shift;
         const float t01 = __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7541)) - shift;
@@ -133,10 +144,11 @@ struct QuadU8 {
 struct QuadF16 {
     static __device__ __forceinline__ float shift_for(float centre) { return centre; }
     static __device__ __forceinline__ float sample(const void *base, int pitch, float u, float v, float shift) {
-        const float fx = floorf(u), fy = floorf(v);
-        const float ax = u - fx, ay = v - fy;
-        const int x0 = (int)fx, y0 = (int)fy;
-        const uint2 w = __ldg(static_cast<const uint2 *>(base) + ((size_t)y0 * pitch + x0));
+        int x0, y0;
+        float ax, ay;
+        split_coord(u, x0, ax);
+        split_coord(v, y0, ay);
+        const uint2 w = __ldg(static_cast<const uint2 *>(base) + (y0 * pitch + x0));
         const float2 r0 = __half22float2(*reinterpret_cast<const __half2 *>(&w.x));
         const float2 r1 = __half22float2(*reinterpret_cast<const __half2 *>(&w.y));
         const float t00 = r0.x - shift, t01 = r0.y - shift, t10 = r1.x - shift, t11 = r1.y - shift;
@@ -145,6 +157,34 @@ struct QuadF16 {
         return fmaf(ay, b - a, a);
     }
 };
+
+// Bilateral window weight exp(-dI^2 / (2 sigma_c^2) - d^2 / (2 sigma_x^2))
+// (PatchMatchCuda.cu:148-149) as exp2 of a pre-scaled exponent:
+// ncf = -log2(e) / (2 sigma_c^2), dk = -log2(e) (dx^2 + dy^2) / (2 sigma_x^2).
+__device__ __forceinline__ float bilateral_weight(float xs, float ncf, float dk) {
+    return exp2f(fmaf(xs * xs, ncf, dk));
+}
+
+// The three standard normals of refinement t (0..5) of one pixel visit:
+// normals 3t..3t+2 of the Box-Muller stream whose pair p uses Philox block
+// p / 2, words (x, y) for even p and (z, w) for odd p.
+__device__ __forceinline__ void refine_normals(uint32_t seed, uint32_t kf, uint32_t pix, uint32_t tag, int t,
+                                               float &ra, float &rb, float &rc) {
+    const int p0 = (3 * t) >> 1;
+    float z[4];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        const int p = p0 + q;
+        const uint4 blk = philox_block(seed, kf, pix, tag, (uint32_t)(p >> 1));
+        const float2 bm = (p & 1) ? box_muller(blk.z, blk.w) : box_muller(blk.x, blk.y);
+        z[2 * q] = bm.x;
+        z[2 * q + 1] = bm.y;
+    }
+    const bool odd = (3 * t) & 1;
+    ra = odd ? z[1] : z[0];
+    rb = odd ? z[2] : z[1];
+    rc = odd ? z[3] : z[2];
+}
 
 // ---------------------------------------------------------------------------
 // One tap of the plane-induced warp for all S sources (PatchMatchCuda.cu:107-157,

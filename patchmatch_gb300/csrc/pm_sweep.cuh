@@ -42,16 +42,18 @@ __device__ __forceinline__ void load_tile(float4 *tile, const float2 *row_trig, 
     }
 }
 
-// Dynamic shared memory of tile_kernel: tile + weights + refinement normals.
-constexpr size_t kTileSmemBytes =
-    sizeof(float4) * kTileRows * kTileCols + sizeof(float) * (kMaxTaps + 18) * kThreads;
+// Dynamic shared memory of tile_kernel: the staged tile only, so that most of
+// the SM's unified L1/shared storage stays L1 for the source-image samples.
+constexpr size_t kTileSmemBytes = sizeof(float4) * kTileRows * kTileCols;
+
+// Resident CTAs per SM the register allocation targets: 3 (80 registers)
+// keeps up to 6 sources spill-free; more sources need the 128-register budget.
+template <int S>
+constexpr int tile_min_blocks() { return S <= 6 ? 3 : 2; }
 
 template <int S, class Img>
-__global__ void __launch_bounds__(kThreads, 3) tile_kernel(const __grid_constant__ SweepArgs a) {
-    extern __shared__ float4 smem_f4[];
-    float4 *tile = smem_f4;
-    float *wsm = reinterpret_cast<float *>(smem_f4 + kTileRows * kTileCols);
-    float *nsm = wsm + kMaxTaps * kThreads;
+__global__ void __launch_bounds__(kThreads, tile_min_blocks<S>()) tile_kernel(const __grid_constant__ SweepArgs a) {
+    extern __shared__ float4 tile[];
 
     const int tid = threadIdx.x, lane = tid & 31, ty = tid >> 5;
     const int x0 = blockIdx.x * kTileW, i0 = blockIdx.y * kTileH;
@@ -70,16 +72,17 @@ __global__ void __launch_bounds__(kThreads, 3) tile_kernel(const __grid_constant
     const int cbase = lane + ((kHaloMax - ph) >> 1);
     const int rbase = ty + kHaloMax - ph;
 
-    // hypothesis-independent part of the window: bilateral weights
-    // w = exp(-(I - I_c)^2 / (2 sigma_c^2) - (dx^2 + dy^2) / (2 sigma_x^2)) (PatchMatchCuda.cu:148-149)
+    // hypothesis-independent moments of the reference window; the bilateral
+    // weights are recomputed per tap in the hypothesis loop (one MUFU.EX2 per
+    // tap, shared by all sources) rather than held in shared memory
     float sw = 0.f, swx = 0.f, swxx = 0.f;
     for (int m1 = 0; m1 < nt; ++m1) {
+        const int k1 = 2 * m1 - ph;
         for (int m2 = 0; m2 < nt; ++m2) {
+            const int k2 = 2 * m2 - ph;
             const float4 e = tile[(rbase + 2 * m1) * kTileCols + cbase + m2];
             const float xs = e.w - Ic;
-            const int k1 = 2 * m1 - ph, k2 = 2 * m2 - ph;
-            const float w = expf(-xs * xs * a.color_factor - (float)(k2 * k2 + k1 * k1) * a.dist_factor);
-            wsm[(m1 * nt + m2) * kThreads + tid] = w;
+            const float w = bilateral_weight(xs, a.ncf, (float)(k1 * k1 + k2 * k2) * a.ndf);
             sw += w;
             swx = fmaf(w, xs, swx);
             swxx = fmaf(w * xs, xs, swxx);
@@ -117,26 +120,10 @@ __global__ void __launch_bounds__(kThreads, 3) tile_kernel(const __grid_constant
                 const float dn = __fadd_rn(__fadd_rn(__fmul_rn(bxc, hx), __fmul_rn(byc, hy)), __fmul_rn(bzc, hz));
                 current_depth = __fdiv_rn(1.0f, fmaxf(1e-6f, fabsf(dn)));
                 cx = hx; cy = hy; cz = hz;
-                // 18 standard normals of this visit: Philox tag sweep + 1
-                // block d gives pairs 2d, 2d+1 = normals 4d .. 4d+3 (18 used)
-                const uint32_t pix = (uint32_t)idx;
-#pragma unroll 1
-                for (int d = 0; d < 5; ++d) {
-                    const uint4 q = philox_block(a.seed, a.keyframe, pix, (uint32_t)(a.sweep + 1), (uint32_t)d);
-                    const float2 z0 = box_muller(q.x, q.y);
-                    nsm[(4 * d) * kThreads + tid] = z0.x;
-                    nsm[(4 * d + 1) * kThreads + tid] = z0.y;
-                    if (d < 4) {
-                        const float2 z1 = box_muller(q.z, q.w);
-                        nsm[(4 * d + 2) * kThreads + tid] = z1.x;
-                        nsm[(4 * d + 3) * kThreads + tid] = z1.y;
-                    }
-                }
             }
-            // refinement t (PatchMatchCuda.cu:364-382)
-            const float ra = nsm[(3 * t) * kThreads + tid];
-            const float rb = nsm[(3 * t + 1) * kThreads + tid];
-            const float rc = nsm[(3 * t + 2) * kThreads + tid];
+            // refinement t (PatchMatchCuda.cu:364-382) with Philox normals (tag sweep + 1)
+            float ra, rb, rc;
+            refine_normals(a.seed, a.keyframe, (uint32_t)idx, (uint32_t)(a.sweep + 1), t, ra, rb, rc);
             depth_hyp = __fmul_rn(current_depth, expf(__fmul_rn(a.depth_range[t], ra)));
             const float nr = a.normal_range[t];
             const float nhx = __fadd_rn(cx, __fmul_rn(nr, ra));
@@ -153,13 +140,15 @@ __global__ void __launch_bounds__(kThreads, 3) tile_kernel(const __grid_constant
 #pragma unroll 1
         for (int m1 = 0; m1 < nt; ++m1) {
             const float4 *trow = tile + (rbase + 2 * m1) * kTileCols + cbase;
-            const float *wrow = wsm + (m1 * nt) * kThreads + tid;
+            const int k1 = 2 * m1 - ph;
+            const float dk1 = (float)(k1 * k1) * a.ndf;
 #pragma unroll 1
             for (int m2 = 0; m2 < nt; ++m2) {
                 const float4 e = trow[m2];
-                const float w = wrow[m2 * kThreads];
-                acc.add(a.P, a.quad, a.qpitch, a.Wf, a.Hf, halfW, halfH, shift, px, py, pz, e.x, e.y, e.z, w,
-                        e.w - Ic);
+                const int k2 = 2 * m2 - ph;
+                const float xs = e.w - Ic;
+                const float w = bilateral_weight(xs, a.ncf, fmaf((float)(k2 * k2), a.ndf, dk1));
+                acc.add(a.P, a.quad, a.qpitch, a.Wf, a.Hf, halfW, halfH, shift, px, py, pz, e.x, e.y, e.z, w, xs);
             }
         }
         float ncc[S];
@@ -221,7 +210,7 @@ __global__ void __launch_bounds__(256) hyp_kernel(const __grid_constant__ HypArg
             const float2 ct = a.col_trig[C];
             const float x = a.ref[(size_t)R * W + C];
             const float xs = x - Ic;
-            const float w = expf(-xs * xs * a.color_factor - (float)(k2 * k2 + k1 * k1) * a.dist_factor);
+            const float w = bilateral_weight(xs, a.ncf, fmaf((float)(k2 * k2), a.ndf, (float)(k1 * k1) * a.ndf));
             sw += w;
             swx = fmaf(w, xs, swx);
             swxx = fmaf(w * xs, xs, swxx);

@@ -37,6 +37,7 @@ struct SweepArgs {
     uint32_t seed, keyframe;
     float color_factor;         // 1 / (2 sigma_color^2)
     float dist_factor;          // 1 / (2 sigma_x^2)
+    float ncf, ndf;             // -log2(e) * color_factor, -log2(e) * dist_factor
     float depth_range[6];       // refinement depth ranges 0.02 * 0.3^t (float, reference rounding)
     float normal_range[6];      // refinement normal ranges 0.5 * 0.8^t
 };
@@ -56,6 +57,7 @@ struct HypArgs {
     int patch_half;
     int combine, top_k;
     float color_factor, dist_factor;
+    float ncf, ndf;
     int n;
     const int2 *ij;
     const float *planes;  // n x 3

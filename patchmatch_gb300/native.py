@@ -22,6 +22,7 @@ MAX_SOURCES = 10
 # Every exported symbol declared in include/pm_gb300.h.
 EXPORTS = (
     "pm_params_default", "pm_create", "pm_destroy", "pm_last_error", "pm_status_string", "pm_launch_count",
+    "pm_stream", "pm_probe_fp32_peak",
     "pm_densify", "pm_request_create", "pm_request_destroy", "pm_request_bytes", "pm_request_set_params",
     "pm_request_set_view", "pm_request_init", "pm_request_set_state", "pm_request_sweep", "pm_request_postprocess",
     "pm_request_run", "pm_request_read", "pm_request_synchronize", "pm_request_depth_device",
@@ -68,6 +69,9 @@ def lib():
     L.pm_status_string.argtypes = [C.c_int]
     L.pm_launch_count.restype = C.c_uint64
     L.pm_launch_count.argtypes = [_vp]
+    L.pm_stream.restype = _vp
+    L.pm_stream.argtypes = [_vp]
+    L.pm_probe_fp32_peak.argtypes = [_vp, C.POINTER(C.c_double)]
     L.pm_densify.argtypes = [_vp, C.c_int, C.c_int, C.POINTER(View), C.c_int, C.POINTER(Params), C.POINTER(Maps)]
     L.pm_request_create.argtypes = [_vp, C.c_int, C.c_int, C.c_int, C.POINTER(Params), C.POINTER(_vp)]
     L.pm_request_destroy.argtypes = [_vp]
@@ -170,6 +174,16 @@ class Context:
     @property
     def launches(self) -> int:
         return int(self._L.pm_launch_count(self.h))
+
+    @property
+    def stream_handle(self) -> int:
+        """cudaStream_t of the context (for torch.cuda.ExternalStream)."""
+        return int(self._L.pm_stream(self.h))
+
+    def probe_fp32_peak(self) -> float:
+        v = C.c_double()
+        self.check(self._L.pm_probe_fp32_peak(self.h, C.byref(v)))
+        return v.value
 
     def last_error(self) -> str:
         return self._L.pm_last_error(self.h).decode()
