@@ -47,9 +47,15 @@ extern "C" {
 #define PM_ENOTBUILT 8   /* no kernel variant for this configuration */
 
 /* view combination (how per-source NCC scores become one cost) */
-#define PM_COMBINE_FOLD 0  /* reference GPU rule: running "average if within 25 %, else max" (PatchMatchCuda.cu:161-171) */
-#define PM_COMBINE_MAX 1   /* reference CPU rule: maximum over sources (depthmap.cc:1104-1127) */
-#define PM_COMBINE_TOPK 2  /* per-pixel view selection: mean of the top_k sources */
+/* PM_COMBINE_FOLD is the reference GPU kernel exactly: its weighted moment
+ * sums are declared once outside the per-view loop and never reset
+ * (PatchMatchCuda.cu:57-62,100-176), so view r's NCC is taken over the samples
+ * of views 1..r together; the running score then averages when within 25 %,
+ * else keeps the max (PatchMatchCuda.cu:93,161-171). */
+#define PM_COMBINE_FOLD 0
+#define PM_COMBINE_MAX 1          /* reference CPU rule: maximum over sources (depthmap.cc:1104-1127) */
+#define PM_COMBINE_TOPK 2         /* per-pixel view selection: mean of the top_k sources */
+#define PM_COMBINE_FOLD_SEPARATE 3 /* the 25 % fold over independent per-source NCCs */
 
 /* longitude seam handling of bilinear source samples */
 #define PM_SEAM_CLAMP 0    /* clamp at the image border (the reference's texture behaviour) */

@@ -16,7 +16,7 @@ BUILD_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD_DIR, "liboracle.so")
 
 OR_MAX_VIEWS = 17
-COMBINE_FOLD, COMBINE_MAX, COMBINE_TOPK = 0, 1, 2
+COMBINE_FOLD, COMBINE_MAX, COMBINE_TOPK, COMBINE_FOLD_SEPARATE = 0, 1, 2, 3
 SEAM_CLAMP, SEAM_WRAP = 0, 1
 ARITH_F64, ARITH_F32_REF = 0, 1
 INTERP_EXACT, INTERP_TEX8_RN, INTERP_TEX8_RZ = 0, 1, 2

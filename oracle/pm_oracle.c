@@ -167,7 +167,19 @@ static float bilinear32(const float *img, int W, int H, float u, float v, int se
 
 /* ------------------------------------------------------------------ */
 /* View combination. */
-static double combine_scores(const double *ncc, int n, int mode, int top_k, int *best)
+static double fold(const double *v, int n)
+{
+    /* PatchMatchCuda.cu:93,161-171: average when within 25 %, else max */
+    double score = -1.0;
+    for (int r = 0; r < n; ++r) {
+        double s2 = v[r];
+        score = (fabs((score - s2) / s2) < 0.25) ? 0.5 * (score + s2) : fmax(score, s2);
+    }
+    return score;
+}
+
+/* ncc: per-view NCCs; cum: NCCs of the moments accumulated over views 0..r */
+static double combine_scores(const double *ncc, const double *cum, int n, int mode, int top_k, int *best)
 {
     int b = 0;
     for (int r = 1; r < n; ++r) if (ncc[r] > ncc[b]) b = r;
@@ -186,28 +198,24 @@ static double combine_scores(const double *ncc, int n, int mode, int top_k, int 
         for (int a = 0; a < k; ++a) acc += s[a];
         return acc / k;
     }
-    /* fold (PatchMatchCuda.cu:93,161-171): average when within 25 %, else max */
-    double score = -1.0;
-    for (int r = 0; r < n; ++r) {
-        double s2 = ncc[r];
-        score = (fabs((score - s2) / s2) < 0.25) ? 0.5 * (score + s2) : fmax(score, s2);
-    }
-    return score;
+    if (mode == OR_COMBINE_FOLD_SEPARATE) return fold(ncc, n);
+    return fold(cum, n);
 }
 
-static float combine_scores_f32(const float *ncc, int n, int mode, int top_k, int *best)
+static float combine_scores_f32(const float *ncc, const float *cum, int n, int mode, int top_k, int *best)
 {
     int b = 0;
     for (int r = 1; r < n; ++r) if (ncc[r] > ncc[b]) b = r;
     if (best) *best = b;
-    if (mode != OR_COMBINE_FOLD) {
+    if (mode == OR_COMBINE_MAX || mode == OR_COMBINE_TOPK) {
         double d[OR_MAX_VIEWS];
         for (int r = 0; r < n; ++r) d[r] = ncc[r];
-        return (float)combine_scores(d, n, mode, top_k, NULL);
+        return (float)combine_scores(d, d, n, mode, top_k, NULL);
     }
+    const float *v = mode == OR_COMBINE_FOLD_SEPARATE ? ncc : cum;
     float score = -1.0f;
     for (int r = 0; r < n; ++r) {
-        float s2 = ncc[r];
+        float s2 = v[r];
         score = (fabsf((score - s2) / s2) < 0.25f) ? (float)(0.5 * (score + s2)) : fmaxf(score, s2);
     }
     return score;
@@ -225,7 +233,8 @@ static double cost_f64(const or_views *v, const or_cost_params *p, int i, int j,
     const double cf = 1.0 / (2.0 * (double)p->sigma_color * (double)p->sigma_color);
     const double df = 1.0 / (2.0 * (double)p->sigma_x * (double)p->sigma_x);
     const double *R0 = v->R[0], *t0 = v->t[0];
-    double ncc[OR_MAX_VIEWS];
+    double ncc[OR_MAX_VIEWS], cum[OR_MAX_VIEWS];
+    double c_sw = 0, c_swx = 0, c_swy = 0, c_swxx = 0, c_swyy = 0, c_swxy = 0;
     const double xc = v->ref[(size_t)i * W + j];
     for (int r = 0; r < v->n_src; ++r) {
         const double *Rr = v->R[r + 1], *tr = v->t[r + 1];
@@ -267,9 +276,13 @@ static double cost_f64(const or_views *v, const or_cost_params *p, int i, int j,
         double mx = swx / sw, my = swy / sw;
         double vx = swxx / sw - mx * mx, vy = swyy / sw - my * my;
         ncc[r] = (vx < 0.1 || vy < 0.1) ? -1.0 : (swxy / sw - mx * my) / sqrt(vx * vy);
+        c_sw += sw; c_swx += swx; c_swy += swy; c_swxx += swxx; c_swyy += swyy; c_swxy += swxy;
+        mx = c_swx / c_sw; my = c_swy / c_sw;
+        vx = c_swxx / c_sw - mx * mx; vy = c_swyy / c_sw - my * my;
+        cum[r] = (vx < 0.1 || vy < 0.1) ? -1.0 : (c_swxy / c_sw - mx * my) / sqrt(vx * vy);
     }
     if (ncc_out) memcpy(ncc_out, ncc, sizeof(double) * v->n_src);
-    return combine_scores(ncc, v->n_src, p->combine, p->top_k, best);
+    return combine_scores(ncc, cum, v->n_src, p->combine, p->top_k, best);
 }
 
 /* Cost, the reference kernel's float arithmetic (PatchMatchCuda.cu:46-180):
@@ -289,13 +302,15 @@ static float cost_f32_ref(const or_views *v, const or_cost_params *p, int i, int
             t1i[y] = (float)(-(R0[0 * 3 + y] * t0[0] + R0[1 * 3 + y] * t0[1] + R0[2 * 3 + y] * t0[2]));
         }
     }
-    float ncc[OR_MAX_VIEWS];
+    float ncc[OR_MAX_VIEWS], cum[OR_MAX_VIEWS];
     const float I_center = v->ref[(size_t)i * W + j];
+    /* the reference declares its sums once, outside the view loop (PatchMatchCuda.cu:57-62) */
+    float sum_x = 0, sum_y = 0, sum_xx = 0, sum_yy = 0, sum_xy = 0, sum_w = 0;
     for (int r = 0; r < v->n_src; ++r) {
         float Rt[9], tt[3];
         for (int a = 0; a < 9; ++a) Rt[a] = (float)v->R[r + 1][a];
         for (int a = 0; a < 3; ++a) tt[a] = (float)v->t[r + 1][a];
-        float sum_x = 0, sum_y = 0, sum_xx = 0, sum_yy = 0, sum_xy = 0, sum_w = 0;
+        float px_ = 0, py_ = 0, pxx = 0, pyy = 0, pxy = 0, pw_ = 0;  /* this view alone */
         for (int k1 = -ph; k1 <= ph; k1 += 2) {
             for (int k2 = -ph; k2 <= ph; k2 += 2) {
                 float I_src = v->ref[(size_t)(i + k1) * W + (j + k2)];
@@ -320,9 +335,11 @@ static float cost_f32_ref(const or_views *v, const or_cost_params *p, int i, int
                 float I_tgt = bilinear32(v->src[r], W, H, u, vv, p->seam, p->interp);
                 float I_diff = I_src - I_center;
                 float w = expf(-I_diff * I_diff * dcolor_factor - (float)(k2 * k2 + k1 * k1) * dx_factor);
-                sum_x += I_src * w; sum_y += I_tgt * w;
-                sum_xx += I_src * I_src * w; sum_yy += I_tgt * I_tgt * w;
-                sum_xy += I_src * I_tgt * w; sum_w += w;
+                sum_x = sum_x + I_src * w; sum_y = sum_y + I_tgt * w;
+                sum_xx = sum_xx + I_src * I_src * w; sum_yy = sum_yy + I_tgt * I_tgt * w;
+                sum_xy = sum_xy + I_src * I_tgt * w; sum_w = sum_w + w;
+                px_ += I_src * w; py_ += I_tgt * w; pxx += I_src * I_src * w;
+                pyy += I_tgt * I_tgt * w; pxy += I_src * I_tgt * w; pw_ += w;
             }
         }
         float prob = 1 / sum_w;
@@ -330,10 +347,15 @@ static float cost_f32_ref(const or_views *v, const or_cost_params *p, int i, int
         float mean_xx = sum_xx * prob, mean_yy = sum_yy * prob, mean_xy = sum_xy * prob;
         float var_x = mean_xx - mean_x * mean_x, var_y = mean_yy - mean_y * mean_y;
         float score_ = (mean_xy - mean_x * mean_y) / sqrtf(var_x * var_y);
+        cum[r] = (var_x < 0.1 || var_y < 0.1) ? -1.0f : score_;
+        prob = 1 / pw_;
+        mean_x = px_ * prob; mean_y = py_ * prob;
+        var_x = pxx * prob - mean_x * mean_x; var_y = pyy * prob - mean_y * mean_y;
+        score_ = (pxy * prob - mean_x * mean_y) / sqrtf(var_x * var_y);
         ncc[r] = (var_x < 0.1 || var_y < 0.1) ? -1.0f : score_;
     }
     if (ncc_out) memcpy(ncc_out, ncc, sizeof(float) * v->n_src);
-    return combine_scores_f32(ncc, v->n_src, p->combine, p->top_k, best);
+    return combine_scores_f32(ncc, cum, v->n_src, p->combine, p->top_k, best);
 }
 
 double or_cost(const or_views *v, const or_cost_params *p, int i, int j,

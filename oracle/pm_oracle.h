@@ -52,7 +52,11 @@ typedef struct {
     double t[OR_MAX_VIEWS][3];
 } or_views;
 
-enum { OR_COMBINE_FOLD = 0, OR_COMBINE_MAX = 1, OR_COMBINE_TOPK = 2 };
+/* OR_COMBINE_FOLD is the reference kernel's rule exactly: its moment sums are
+ * never reset between views (PatchMatchCuda.cu:57-62,100-176), so view r's
+ * NCC covers the samples of views 1..r, folded with the 25 % rule.
+ * OR_COMBINE_FOLD_SEPARATE folds independent per-view NCCs instead. */
+enum { OR_COMBINE_FOLD = 0, OR_COMBINE_MAX = 1, OR_COMBINE_TOPK = 2, OR_COMBINE_FOLD_SEPARATE = 3 };
 enum { OR_SEAM_CLAMP = 0, OR_SEAM_WRAP = 1 };
 /* OR_ARITH_F64: exact (double) arithmetic and exact bilinear interpolation.
  * OR_ARITH_F32_REF: the reference kernel's own float arithmetic, step by step

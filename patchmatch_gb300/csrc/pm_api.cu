@@ -168,7 +168,7 @@ int validate_params(pm_ctx *ctx, const pm_params *p) {
     if (p->patch_half != 1 && p->patch_half != 3 && p->patch_half != 5)
         return fail(ctx, PM_EINVAL, "patch_half must be 1, 3 or 5 (got %d)", p->patch_half);
     if (p->iterations < 0 || p->iterations > 1000) return fail(ctx, PM_EINVAL, "iterations out of range");
-    if (p->combine < PM_COMBINE_FOLD || p->combine > PM_COMBINE_TOPK) return fail(ctx, PM_EINVAL, "bad combine");
+    if (p->combine < PM_COMBINE_FOLD || p->combine > PM_COMBINE_FOLD_SEPARATE) return fail(ctx, PM_EINVAL, "bad combine");
     if (p->top_k < 1) return fail(ctx, PM_EINVAL, "top_k must be >= 1");
     if (p->seam != PM_SEAM_CLAMP && p->seam != PM_SEAM_WRAP) return fail(ctx, PM_EINVAL, "bad seam");
     if (p->init_mode != PM_INIT_LOGUNIFORM_HEMI && p->init_mode != PM_INIT_REF_UNIFORM)

@@ -109,14 +109,13 @@ __device__ __forceinline__ float lat_halfturns(float x, float y, float z) {
 // sample is one aligned load.  Texel k sits at coordinate k, matching the
 // reference's texture reads at u + 0.5 (PatchMatchCuda.cu:146).
 // ---------------------------------------------------------------------------
-// Split a coordinate c in [0, 2^22) into a cell index k and weight a in
-// [0, 1] with c = k + a, without conversion instructions: adding
-// 2^23 - 1/2 rounds c - 1/2 to an integer in the low mantissa bits.  At odd
-// integer c this gives k = c - 1, a = 1, which samples the same texel value.
+// Split a sample coordinate c in [0, N] into cell index k = floor(c) and
+// weight a = c - k.  A NaN coordinate (a degenerate plane hypothesis) gives
+// k = 0, so every index stays inside the (N+1)-entry quad array.
 __device__ __forceinline__ void split_coord(float c, int &k, float &a) {
-    const float m = c + 8388607.5f;
-    k = (int)(__float_as_uint(m) & 0x7FFFFFu);
-    a = c - (m - 8388608.0f);
+    const float f = floorf(c);
+    k = (int)f;
+    a = c - f;
 }
 
 struct QuadU8 {
@@ -243,51 +242,81 @@ __device__ __forceinline__ float ncc_from_moments(float sw, float swx, float swx
     return (vx < 0.1f || vy < 0.1f) ? -1.0f : ncc;
 }
 
-// View combination of S per-source scores; best = argmax source.
-//  PM_COMBINE_FOLD: the reference's running "average when within 25 %, else
-//    max", starting from -1 (PatchMatchCuda.cu:93,171), folded over sources in order;
+// View combination; best = argmax of the per-source NCCs (sep).
+//  PM_COMBINE_FOLD: the reference GPU kernel: NCC of the moments accumulated
+//    over sources 0..r (cum[r], the reference never resets its sums between
+//    views, PatchMatchCuda.cu:57-62,100-176), folded from -1 with "average
+//    when within 25 %, else max" (PatchMatchCuda.cu:93,171);
+//  PM_COMBINE_FOLD_SEPARATE: the same fold over the per-source NCCs;
 //  PM_COMBINE_MAX: maximum (the reference CPU path, depthmap.cc:1104-1127);
 //  PM_COMBINE_TOPK: mean of the top_k best sources (per-pixel view selection).
 template <int S>
-__device__ __forceinline__ float combine_scores(const float (&ncc)[S], int mode, int top_k, int *best) {
-    int b = 0;
-#pragma unroll
-    for (int r = 1; r < S; ++r) b = (ncc[r] > ncc[b]) ? r : b;
-    *best = b;
-    if (mode == PM_COMBINE_MAX) {
-        float m = ncc[0];
-#pragma unroll
-        for (int r = 1; r < S; ++r) m = fmaxf(m, ncc[r]);
-        return m;
-    }
-    if (mode == PM_COMBINE_TOPK) {
-        // sum of the k largest: repeated selection over a small register array
-        float v[S];
-#pragma unroll
-        for (int r = 0; r < S; ++r) v[r] = ncc[r];
-        const int k = top_k < 1 ? 1 : (top_k > S ? S : top_k);
-        float accf = 0.0f;  // summed in descending order
-        for (int a = 0; a < k; ++a) {
-            int bi = 0;
-#pragma unroll
-            for (int r = 1; r < S; ++r) bi = (v[r] > v[bi]) ? r : bi;
-            float m = v[0];
-#pragma unroll
-            for (int r = 0; r < S; ++r) m = (r == bi) ? v[r] : m;
-            accf += m;
-#pragma unroll
-            for (int r = 0; r < S; ++r) v[r] = (r == bi) ? -3.0e38f : v[r];
-        }
-        return accf / (float)k;
-    }
+__device__ __forceinline__ float fold_scores(const float (&v)[S]) {
     float score = -1.0f;
 #pragma unroll
     for (int r = 0; r < S; ++r) {
-        const float s2 = ncc[r];
+        const float s2 = v[r];
         score = (fabsf(__fdiv_rn(__fsub_rn(score, s2), s2)) < 0.25f) ? __fmul_rn(0.5f, __fadd_rn(score, s2))
                                                                      : fmaxf(score, s2);
     }
     return score;
+}
+
+template <int S>
+__device__ __forceinline__ float combine_scores(const float (&sep)[S], const float (&cum)[S], int mode, int top_k,
+                                                int *best) {
+    int b = 0;
+#pragma unroll
+    for (int r = 1; r < S; ++r) b = (sep[r] > sep[b]) ? r : b;
+    *best = b;
+    if (mode == PM_COMBINE_FOLD) return fold_scores<S>(cum);
+    if (mode == PM_COMBINE_FOLD_SEPARATE) return fold_scores<S>(sep);
+    if (mode == PM_COMBINE_MAX) {
+        float m = sep[0];
+#pragma unroll
+        for (int r = 1; r < S; ++r) m = fmaxf(m, sep[r]);
+        return m;
+    }
+    // PM_COMBINE_TOPK: sum of the k largest by repeated selection
+    float v[S];
+#pragma unroll
+    for (int r = 0; r < S; ++r) v[r] = sep[r];
+    const int k = top_k < 1 ? 1 : (top_k > S ? S : top_k);
+    float accf = 0.0f;  // summed in descending order
+    for (int a = 0; a < k; ++a) {
+        int bi = 0;
+#pragma unroll
+        for (int r = 1; r < S; ++r) bi = (v[r] > v[bi]) ? r : bi;
+        float m = v[0];
+#pragma unroll
+        for (int r = 0; r < S; ++r) m = (r == bi) ? v[r] : m;
+        accf += m;
+#pragma unroll
+        for (int r = 0; r < S; ++r) v[r] = (r == bi) ? -3.0e38f : v[r];
+    }
+    return accf / (float)k;
+}
+
+// Per-source and cumulative NCCs of one hypothesis from the window moments.
+template <int S, class Img>
+__device__ __forceinline__ void source_nccs(const TapAccum<S, Img> &acc, float sw, float swx, float swxx, int mode,
+                                            float (&sep)[S], float (&cum)[S]) {
+#pragma unroll
+    for (int r = 0; r < S; ++r) sep[r] = ncc_from_moments(sw, swx, swxx, acc.swy[r], acc.swyy[r], acc.swxy[r]);
+    if (mode == PM_COMBINE_FOLD) {
+        float cy = 0.f, cyy = 0.f, cxy = 0.f;
+#pragma unroll
+        for (int r = 0; r < S; ++r) {
+            cy += acc.swy[r];
+            cyy += acc.swyy[r];
+            cxy += acc.swxy[r];
+            const float n = (float)(r + 1);
+            cum[r] = ncc_from_moments(n * sw, n * swx, n * swxx, cy, cyy, cxy);
+        }
+    } else {
+#pragma unroll
+        for (int r = 0; r < S; ++r) cum[r] = sep[r];
+    }
 }
 
 }  // namespace pm

@@ -151,11 +151,10 @@ __global__ void __launch_bounds__(kThreads, tile_min_blocks<S>()) tile_kernel(co
                 acc.add(a.P, a.quad, a.qpitch, a.Wf, a.Hf, halfW, halfH, shift, px, py, pz, e.x, e.y, e.z, w, xs);
             }
         }
-        float ncc[S];
-#pragma unroll
-        for (int r = 0; r < S; ++r) ncc[r] = ncc_from_moments(sw, swx, swxx, acc.swy[r], acc.swyy[r], acc.swxy[r]);
+        float sep[S], cum[S];
+        source_nccs<S, Img>(acc, sw, swx, swxx, a.combine, sep, cum);
         int hb;
-        float sc = combine_scores<S>(ncc, a.combine, a.top_k, &hb);
+        float sc = combine_scores<S>(sep, cum, a.combine, a.top_k, &hb);
 
         if (a.mode == kModeScore) {
             score = sc;
@@ -218,14 +217,13 @@ __global__ void __launch_bounds__(256) hyp_kernel(const __grid_constant__ HypArg
                     rt.x * ct.y, w, xs);
         }
     }
-    float ncc[S];
+    float sep[S], cum[S];
+    source_nccs<S, Img>(acc, sw, swx, swxx, a.combine, sep, cum);
+    if (a.per_source)
 #pragma unroll
-    for (int r = 0; r < S; ++r) {
-        ncc[r] = ncc_from_moments(sw, swx, swxx, acc.swy[r], acc.swyy[r], acc.swxy[r]);
-        if (a.per_source) a.per_source[(size_t)h * S + r] = ncc[r];
-    }
+        for (int r = 0; r < S; ++r) a.per_source[(size_t)h * S + r] = sep[r];
     int hb;
-    const float sc = combine_scores<S>(ncc, a.combine, a.top_k, &hb);
+    const float sc = combine_scores<S>(sep, cum, a.combine, a.top_k, &hb);
     if (a.scores) a.scores[h] = sc;
     if (a.best) a.best[h] = hb;
 }

@@ -13,7 +13,7 @@ import numpy as np
 from ._native import load_pm_lib
 
 PM_OK, PM_EINVAL, PM_ENOMEM, PM_EBUDGET, PM_ETIMEOUT, PM_ECUDA, PM_ENOTREADY, PM_ECANCELLED, PM_ENOTBUILT = range(9)
-COMBINE_FOLD, COMBINE_MAX, COMBINE_TOPK = 0, 1, 2
+COMBINE_FOLD, COMBINE_MAX, COMBINE_TOPK, COMBINE_FOLD_SEPARATE = 0, 1, 2, 3
 SEAM_CLAMP, SEAM_WRAP = 0, 1
 INIT_LOGUNIFORM_HEMI, INIT_REF_UNIFORM = 0, 1
 IMAGE_U8, IMAGE_F16 = 0, 1

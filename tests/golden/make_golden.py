@@ -13,7 +13,8 @@ small fixtures that the CPU tests replay against the oracle:
     probe_xy (n, 2), probe (n,) linear-filtered texture reads of source 1 past
                                 the image borders (the hardware border policy)
 
-    python tests/golden/make_golden.py      (needs a GPU and the fatbin)
+    python tests/golden/make_golden.py [out_dir]     (needs a GPU and the fatbin;
+                                                      default out_dir: tests/golden)
 """
 import os
 import sys
@@ -53,7 +54,9 @@ def main():
     xs = np.array([-1.0, -0.5, 0.0, 0.25, 0.5, 1.0, 126.5, 127.0, 127.25, 127.5, 127.75, 128.0, 128.5, 129.0, 130.0])
     probe_xy = np.stack(np.meshgrid(xs, np.array([10.5, 30.25])), -1).reshape(-1, 2).astype(np.float32)
     probe = rk.probe_texture(1, probe_xy)
-    out = os.path.join(HERE, "ref_kernels_128x64.npz")
+    out_dir = sys.argv[1] if len(sys.argv) > 1 else HERE
+    os.makedirs(out_dir, exist_ok=True)
+    out = os.path.join(out_dir, "ref_kernels_128x64.npz")
     np.savez_compressed(out, images=np.stack(imgs), R=req.R, t=req.t, bearings=bearings, planes=planes,
                         scores=scores, probe_xy=probe_xy, probe=probe)
     print("wrote", out)

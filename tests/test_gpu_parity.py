@@ -42,7 +42,8 @@ def _req_on_gpu(ctx, req, **kw):
     return r
 
 
-@pytest.mark.parametrize("combine", [native.COMBINE_FOLD, native.COMBINE_MAX, native.COMBINE_TOPK])
+@pytest.mark.parametrize("combine", [native.COMBINE_FOLD, native.COMBINE_MAX, native.COMBINE_TOPK,
+                                     native.COMBINE_FOLD_SEPARATE])
 def test_fixed_hypotheses_match_fp64_oracle(ctx, room, combine):
     """Per-source NCC of 20k fixed hypotheses: |gpu - fp64| <= 1e-5 * max(1, |ncc|)
     for >= 99.5 % and <= 1e-3 for all (rare tails come from FP32 coordinates of

@@ -74,6 +74,11 @@ def test_combine_modes(room):
     assert np.isclose(mx[0], ncc[0].max()) and b[0] == int(np.argmax(ncc[0]))
     tk, _ = O.cost_batch(V, O.cost_params(combine=O.COMBINE_TOPK, top_k=2), ij, pl)
     assert np.isclose(tk[0], np.sort(ncc[0])[::-1][:2].mean())
+    fs, _ = O.cost_batch(V, O.cost_params(combine=O.COMBINE_FOLD_SEPARATE), ij, pl)
+    score = -1.0
+    for s2 in ncc[0]:
+        score = 0.5 * (score + s2) if abs((score - s2) / s2) < 0.25 else max(score, s2)
+    assert np.isclose(fs[0], score)
 
 
 def test_median3_replicate_border():

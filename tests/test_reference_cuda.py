@@ -47,9 +47,8 @@ def test_reference_cost_matches_oracle_tex8(rk):
         o, _ = O.cost_batch(V, O.cost_params(arith=O.ARITH_F32_REF, interp=interp), ij, P[ii, jj])
         errs[interp] = np.abs(o - ref[ii, jj])
         print(f"interp {interp}: median {np.median(errs[interp]):.2e} p99 {np.quantile(errs[interp], .99):.2e}")
-    best = min(errs, key=lambda k: np.median(errs[k]))
-    assert best != O.INTERP_EXACT
-    assert np.median(errs[best]) < 1e-4
+    assert min(errs, key=lambda k: np.median(errs[k])) == O.INTERP_TEX8_RN
+    assert np.median(errs[O.INTERP_TEX8_RN]) < 1e-4
 
 
 def test_converged_depth_agrees_with_reference_gpu_path(rk, ctx):
