@@ -204,6 +204,33 @@ typedef struct {
 int pm_fuse(pm_ctx *ctx, int width, int height, int n_views, float *const *depths, const double *R_cw,
             const double *t_cw, const uint8_t *bgr, float same_depth_threshold, float *pruned, pm_points *out);
 
+/* ---- fusion for callers that cannot allocate device memory ----
+ * Some callers must not allocate at the moment they fuse: a process whose
+ * device memory belongs to an external pool or arena, a real-time thread that
+ * cannot enter the CUDA allocator (unbounded latency, possible device-wide
+ * synchronisation), or code whose HBM is already committed.  This entry point
+ * has no counterpart in the reference.  It runs the pm_fuse kernels on
+ * caller-owned DEVICE buffers and enqueues on `stream` (a cudaStream_t, NULL =
+ * default stream) without synchronising; it never calls cudaMalloc/cudaFree.
+ * Its working memory is one file-scope device array (about 20 MB) that every
+ * GPU loading the library holds until the process exits, so images are limited
+ * to PM_FUSE_NOALLOC_MAX_PIXELS pixels, width <= PM_FUSE_NOALLOC_MAX_WIDTH and
+ * height <= PM_FUSE_NOALLOC_MAX_HEIGHT (larger sizes return PM_EINVAL).
+ * The first call on each device looks up that array's device address
+ * (cudaGetSymbolAddress) with the device current; make that first call before
+ * any stream capture.  All calls on a device share the array: calls whose GPU
+ * work overlaps (e.g. on two streams) race and must be serialised by the
+ * caller.  depths[k] (device, H x W floats, k = 0 head) are edited in place as
+ * by pm_fuse; pruned (H x W), xyz (H*W x 3 floats, world frame), bgr_out
+ * (H*W x 3, may be NULL), ij (H*W x 2, may be NULL) and count (one unsigned)
+ * are device outputs; bgr (device, may be NULL) is the head's colour image. */
+#define PM_FUSE_NOALLOC_MAX_PIXELS (1u << 21)
+#define PM_FUSE_NOALLOC_MAX_WIDTH 8192
+#define PM_FUSE_NOALLOC_MAX_HEIGHT 4096
+int pm_fuse_noalloc(int width, int height, int n_views, float *const *depths, const double *R_cw,
+                    const double *t_cw, const uint8_t *bgr, float same_depth_threshold, float *pruned, float *xyz,
+                    uint8_t *bgr_out, int32_t *ij, unsigned *count, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -43,7 +43,7 @@ def _sources():
     deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     deps += [os.path.join(INC, f) for f in os.listdir(INC)]
     units = []
-    for f in ("pm_api.cu", "pm_prep.cu", "pm_post.cu", "pm_dense.cpp"):
+    for f in ("pm_api.cu", "pm_prep.cu", "pm_post.cu", "pm_fuse_noalloc.cu", "pm_dense.cpp"):
         units.append((os.path.join(CSRC, f), os.path.join(OBJ_DIR, os.path.splitext(f)[0] + ".o"), []))
     for s in range(1, MAX_SOURCES + 1):
         units.append((os.path.join(CSRC, "pm_inst.cu"), os.path.join(OBJ_DIR, f"pm_inst_s{s}.o"),

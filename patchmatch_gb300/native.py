@@ -26,7 +26,7 @@ EXPORTS = (
     "pm_densify", "pm_request_create", "pm_request_destroy", "pm_request_bytes", "pm_request_set_params",
     "pm_request_set_view", "pm_request_init", "pm_request_set_state", "pm_request_sweep", "pm_request_postprocess",
     "pm_request_run", "pm_request_read", "pm_request_synchronize", "pm_request_depth_device",
-    "pm_score_hypotheses", "pm_filter_consistency", "pm_fuse",
+    "pm_score_hypotheses", "pm_filter_consistency", "pm_fuse", "pm_fuse_noalloc",
 )
 
 
@@ -92,6 +92,8 @@ def lib():
     L.pm_filter_consistency.argtypes = [_vp, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, C.c_int, C.c_float,
                                         C.c_int, C.c_float, _vp]
     L.pm_fuse.argtypes = [_vp, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, C.c_float, _vp, C.POINTER(Points)]
+    L.pm_fuse_noalloc.argtypes = [C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, C.c_float, _vp, _vp, _vp, _vp, _vp,
+                                  _vp]
     L._pm_typed = True
     return L
 
