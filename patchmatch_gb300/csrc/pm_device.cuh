@@ -130,12 +130,13 @@ struct QuadU8 {
         split_coord(v, y0, ay);
         const uint32_t w = __ldg(static_cast<const uint32_t *>(base) + (y0 * pitch + x0));
         // bytes -> floats minus the centre intensity: (2^23 + byte) - (2^23 + c)
-        const float t00 = __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540)) - shift;
-        const float t01 = __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7541)) - shift;
-        const float t10 = __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7542)) - shift;
-        const float t11 = __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7543)) - shift;
-        const float a = fmaf(ax, t01 - t00, t00);
-        const float b = fmaf(ax, t11 - t10, t10);
+        // texels as 2^23 + byte; differences are exact, the shift is applied once per row
+        const float m00 = __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540));
+        const float m01 = __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7541));
+        const float m10 = __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7542));
+        const float m11 = __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7543));
+        const float a = fmaf(ax, m01 - m00, m00 - shift);
+        const float b = fmaf(ax, m11 - m10, m10 - shift);
         return fmaf(ay, b - a, a);
     }
 };
@@ -213,14 +214,20 @@ struct TapAccum {
         const float sbx = __uint_as_float(__float_as_uint(bx) ^ sg);
         const float sby = __uint_as_float(__float_as_uint(by) ^ sg);
         const float sbz = __uint_as_float(__float_as_uint(bz) ^ sg);
+        // phase 1: all S sample coordinates, so the S footprint loads issue
+        // back to back; phase 2: bilinear + moments as they arrive
+        float u[S], v[S];
 #pragma unroll
         for (int r = 0; r < S; ++r) {
             const float X = fmaf(P.M[r][0], sbx, fmaf(P.M[r][1], sby, fmaf(P.M[r][2], sbz, as * P.c[r][0])));
             const float Y = fmaf(P.M[r][3], sbx, fmaf(P.M[r][4], sby, fmaf(P.M[r][5], sbz, as * P.c[r][1])));
             const float Z = fmaf(P.M[r][6], sbx, fmaf(P.M[r][7], sby, fmaf(P.M[r][8], sbz, as * P.c[r][2])));
-            const float u = fmaf(Wf, lon_turns(X, Z), halfW);
-            const float v = fmaf(Hf, lat_halfturns(X, Y, Z), halfH);
-            const float y = Img::sample(quad[r], qpitch, u, v, shift);
+            u[r] = fmaf(Wf, lon_turns(X, Z), halfW);
+            v[r] = fmaf(Hf, lat_halfturns(X, Y, Z), halfH);
+        }
+#pragma unroll
+        for (int r = 0; r < S; ++r) {
+            const float y = Img::sample(quad[r], qpitch, u[r], v[r], shift);
             const float wy = w * y;
             swy[r] += wy;
             swyy[r] = fmaf(wy, y, swyy[r]);

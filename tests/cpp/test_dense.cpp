@@ -20,7 +20,7 @@
     } while (0)
 
 int main() {
-    const int W = 512, H = 256, N = 9;
+    const int W = 512, H = 256, N = 12;
     pm_scene *sc = pm_scene_create(PM_SCENE_ROOM_OBJECTS, 7);
     CHECK(sc);
     std::vector<dense::Matx33d> Rs(N);
@@ -30,7 +30,7 @@ int main() {
     std::vector<std::vector<float>> gts(N);
     for (int k = 0; k < N; ++k) {
         double R[9], t[3];
-        CHECK(pm_scene_trajectory_pose(sc, 3, 8, 10.0, 0.4 + 0.25 * k, R, t) == 0);
+        CHECK(pm_scene_trajectory_pose(sc, 3, 8, 10.0, 0.4 + 0.2 * k, R, t) == 0);
         for (int a = 0; a < 9; ++a) Rs[k][a] = R[a];
         for (int a = 0; a < 3; ++a) ts[k][a] = t[a];
         grays[k] = dense::MatU8(H, W);
@@ -103,6 +103,7 @@ int main() {
     }
     CHECK(estimated == N - 2);
     CHECK(cleaned == N - 2 - 4);
+    CHECK(pruned_sets == cleaned - 4 && points > 0);
     std::printf("estimated %d cleaned %d pruned %d points %zu mean acc2%% %.3f\n", estimated, cleaned, pruned_sets,
                 points, acc_sum / estimated);
     CHECK(acc_sum / estimated > 0.6);

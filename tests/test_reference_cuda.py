@@ -52,27 +52,37 @@ def test_reference_cost_matches_oracle_tex8(rk):
 
 
 def test_converged_depth_agrees_with_reference_gpu_path(rk, ctx):
-    """Full runs at 512x256 with the reference's two sources and fold rule:
-    fraction of pixels valid in both whose depths agree within 1 %."""
+    """Full runs at 512x256 with the reference's two sources and fold rule,
+    both post-filtered as the reference host does (depthmap.cc:731-767).
+    The reference's own runs differ from each other (clock-seeded cuRAND), so
+    its run-to-run agreement is the floor: ours must agree with it as well as
+    it agrees with itself, and be at least as accurate against the truth."""
     req = scene.make_request(scene.ROOM, 512, 256, 2, seed=32)
     imgs = [v.gray_u8 for v in req.views]
     rk.setup([im.astype(np.float32) for im in imgs], req.R, req.t)
     iters = 8
-    ref = rk.run(iters, 0.3, 20.0)
-    p = native.default_params(iterations=iters, postprocess=0, init_mode=native.INIT_REF_UNIFORM)
+    ref_f = []
+    for _ in range(2):
+        raw = rk.run(iters, 0.3, 20.0)
+        d, _ = O.postprocess(imgs[0].astype(np.float32), raw["depth"], raw["score"], min_depth=0.3, max_depth=20.0)
+        ref_f.append(d)
+    p = native.default_params(iterations=iters, init_mode=native.INIT_REF_UNIFORM)
     r = ctx.request(512, 256, 2, p)
     r.set_views(imgs, req.R, req.t)
     r.run()
-    ours = r.read(raw=True)
+    ours = r.read()["depth"]
     gt = req.views[0].depth
-    m = np.zeros((256, 512), bool)
-    m[6:251, 6:507] = True
-    # pixels both methods resolved (score above the post-filter's 0.1 floor)
-    both = m & (ref["score"] > 0.1) & (ours["score"] > 0.1)
-    agree = (np.abs(ours["depth"] - ref["depth"]) / ref["depth"] < 0.01)[both].mean()
-    acc_ref = (np.abs(ref["depth"] - gt) / gt < 0.01)[both].mean()
-    acc_ours = (np.abs(ours["depth"] - gt) / gt < 0.01)[both].mean()
-    print(f"resolved {both.mean():.3f} agree1% {agree:.4f} ref-acc1% {acc_ref:.4f} ours-acc1% {acc_ours:.4f}")
-    assert agree >= 0.9
-    assert acc_ours >= acc_ref - 0.02
+
+    def agree(a, b):
+        both = (a > 0) & (b > 0)
+        return (np.abs(a - b) / b < 0.01)[both].mean(), both.mean()
+
+    rr, rr_cov = agree(ref_f[1], ref_f[0])
+    orf, or_cov = agree(ours, ref_f[0])
+    acc = lambda d: (np.abs(d - gt) / gt < 0.01)[d > 0].mean()
+    print(f"ref-vs-ref agree1% {rr:.4f} (both valid {rr_cov:.3f}); ours-vs-ref {orf:.4f} ({or_cov:.3f}); "
+          f"acc1% ref {acc(ref_f[0]):.4f} ours {acc(ours):.4f}; valid ref {(ref_f[0] > 0).mean():.3f} "
+          f"ours {(ours > 0).mean():.3f}")
+    assert orf >= 0.95 * rr
+    assert acc(ours) >= acc(ref_f[0]) - 0.02
     r.close()
