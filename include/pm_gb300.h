@@ -157,6 +157,16 @@ int pm_request_init(pm_request *req);
  * seeding entry for prior knowledge (replaces the host round trip of
  * depthmap.cc:669-719). scores may be NULL (then every interior pixel is rescored). */
 int pm_request_set_state(pm_request *req, const float *planes, const float *scores);
+/* Reuse a previous keyframe's post-filtered result as initialisation: its
+ * planes are splatted into this view (nearest candidate per pixel) and kept
+ * where they score higher than the random planes.  pm_request_seed does it
+ * now (after pm_request_init); pm_request_set_prior makes pm_request_run do
+ * it after the random initialisation (NULL clears).  The prior must stay
+ * alive and unchanged until the work is done.  Replaces the host
+ * PreInitResultWarp (depthmap.cc:434-516); the prior's normals are rotated
+ * into the new camera (the reference reuses them unrotated). */
+int pm_request_seed(pm_request *req, const pm_request *prior);
+int pm_request_set_prior(pm_request *req, const pm_request *prior);
 /* n_half red/black half-sweeps starting at half-sweep index first_half
  * (even = red, odd = black; sweep = first_half / 2).  Replaces
  * PatchMatchRedBlackPass (PatchMatchCuda.cu:568-615). */

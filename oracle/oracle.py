@@ -78,6 +78,7 @@ def lib():
         L.or_sweeps.argtypes = [C.POINTER(ORViews), C.POINTER(ORRunParams), _fp, _fp, _fp, _ip, C.c_int, C.c_int]
         L.or_postprocess.argtypes = [C.c_int, C.c_int, C.c_int, _fp, _u8p, C.c_float, C.c_float, C.c_float,
                                      C.c_float, _fp, _fp]
+        L.or_warp_prior.argtypes = [C.c_int, C.c_int, _fp, _fp, _dp, _dp, C.c_int, C.c_int, _dp, _dp, _fp]
         L.or_median3.argtypes = [C.c_int, C.c_int, _fp, _fp]
         L.or_clean.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(_fp), _dp, _dp, C.c_int, C.c_float,
                                C.c_int, C.c_float, _fp]
@@ -171,6 +172,18 @@ def postprocess(ref, depth, score, patch_half=5, mask=None, min_patch_sd=0.0, mi
     lib().or_postprocess(W, H, patch_half, _p(r, _fp), _p(m, _u8p), min_patch_sd, min_depth, max_depth,
                          min_score, _p(d, _fp), _p(s, _fp))
     return d, s
+
+
+def warp_prior(prev_plane, prev_depth, Rp, tp, W, H, Rn, tn):
+    """Seeding candidates (H, W, 4): plane xyz + range (0 = none)."""
+    Hp, Wp = prev_depth.shape
+    pl = np.ascontiguousarray(prev_plane, np.float32)
+    d = np.ascontiguousarray(prev_depth, np.float32)
+    Rp, tp, Rn, tn = [np.ascontiguousarray(a, np.float64) for a in (Rp, tp, Rn, tn)]
+    cand = np.zeros((H, W, 4), np.float32)
+    lib().or_warp_prior(Wp, Hp, _p(pl, _fp), _p(d, _fp), _p(Rp, _dp), _p(tp, _dp), W, H, _p(Rn, _dp), _p(tn, _dp),
+                        _p(cand, _fp))
+    return cand
 
 
 def median3(x):

@@ -653,6 +653,63 @@ void or_postprocess(int W, int H, int patch_half, const float *ref, const uint8_
 }
 
 /* ------------------------------------------------------------------ */
+/* Seeding candidates from a prior result (PreInitResultWarp, depthmap.cc:434-516):
+ * lift each valid prior pixel onto its plane (PosPatchPartOnPlane :163-177),
+ * move it into the new camera, round to the nearest pixel; the nearest splat
+ * (then the lowest prior index) wins a pixel.  The prior's unit normal is
+ * rotated into the new camera (the reference reuses it unrotated).  cand:
+ * H*W*4 (plane xyz, range; range 0 = none). */
+void or_warp_prior(int Wp, int Hp, const float *prev_plane, const float *prev_depth, const double *Rp,
+                   const double *tp, int W, int H, const double *Rn, const double *tn, float *cand)
+{
+    double M[9], c[3];
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b)
+            M[3 * a + b] = Rn[3 * a] * Rp[3 * b] + Rn[3 * a + 1] * Rp[3 * b + 1] + Rn[3 * a + 2] * Rp[3 * b + 2];
+    for (int a = 0; a < 3; ++a) c[a] = tn[a] - (M[3 * a] * tp[0] + M[3 * a + 1] * tp[1] + M[3 * a + 2] * tp[2]);
+    const size_t N = (size_t)W * H;
+    double *best_r = (double *)malloc(N * sizeof(double));
+    long *best_i = (long *)malloc(N * sizeof(long));
+    for (size_t q = 0; q < N; ++q) { best_r[q] = INFINITY; best_i[q] = -1; cand[4 * q + 3] = 0.0f; }
+    for (int i = 0; i < Hp; ++i)
+        for (int j = 0; j < Wp; ++j) {
+            size_t idx = (size_t)i * Wp + j;
+            if (!(prev_depth[idx] >= 1e-4f)) continue;
+            const float *pl = prev_plane + 3 * idx;
+            double b[3];
+            or_bearing64(Wp, Hp, i, j, b);
+            double sc = pl[0] * b[0] + pl[1] * b[1] + pl[2] * b[2];
+            if (sc < 1e-6 && sc >= 0) sc = 1e-6;
+            else if (sc > -1e-6 && sc < 0) sc = -1e-6;
+            double P[3] = {b[0] / sc, b[1] / sc, b[2] / sc}, X[3];
+            for (int a = 0; a < 3; ++a) X[a] = M[3 * a] * P[0] + M[3 * a + 1] * P[1] + M[3 * a + 2] * P[2] + c[a];
+            double r = sqrt(X[0] * X[0] + X[1] * X[1] + X[2] * X[2]);
+            if (!(r >= 1e-4) || !isfinite(r)) continue;
+            double lon = atan2(X[0], X[2]), lat = -asin(fmin(1.0, fmax(-1.0, X[1] / r)));
+            double x = W * (0.5 + lon / (2 * PI_D)), y = H * (0.5 - lat / PI_D);
+            int ti = (int)(y + 0.5), tj = (int)(x + 0.5);
+            if (ti < 0 || tj < 0 || ti >= H || tj >= W) continue;
+            size_t t = (size_t)ti * W + tj;
+            float rf = (float)r;
+            if (rf < best_r[t] || (rf == best_r[t] && (long)idx < best_i[t])) {
+                best_r[t] = rf; best_i[t] = (long)idx;
+                double nn = 1.0 / sqrt((double)pl[0] * pl[0] + (double)pl[1] * pl[1] + (double)pl[2] * pl[2]);
+                double n[3];
+                for (int a = 0; a < 3; ++a) n[a] = (M[3 * a] * pl[0] + M[3 * a + 1] * pl[1] + M[3 * a + 2] * pl[2]) * nn;
+                double bn[3];
+                or_bearing64(W, H, ti, tj, bn);
+                double den = r * (n[0] * bn[0] + n[1] * bn[1] + n[2] * bn[2]);
+                if (den < 1e-5 && den >= 0) den = 1e-5;
+                else if (den > -1e-5 && den < 0) den = -1e-5;
+                for (int a = 0; a < 3; ++a) cand[4 * t + a] = (float)(n[a] / den);
+                cand[4 * t + 3] = rf;
+            }
+        }
+    free(best_r);
+    free(best_i);
+}
+
+/* ------------------------------------------------------------------ */
 /* Reprojection helpers of the reference host code (depthmap.cc:143-161). */
 
 static void mat_t_vec(const double *R, const double *x, double *y)

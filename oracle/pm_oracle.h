@@ -135,6 +135,10 @@ void or_postprocess(int W, int H, int patch_half, const float *ref,
 /* OpenCV medianBlur(ksize 3, BORDER_REPLICATE) restated, float maps. */
 void or_median3(int W, int H, const float *in, float *out);
 
+/* ---- seeding from a prior result (depthmap.cc:434-516) ---- */
+void or_warp_prior(int Wp, int Hp, const float *prev_plane, const float *prev_depth, const double *Rp,
+                   const double *tp, int W, int H, const double *Rn, const double *tn, float *cand);
+
 /* ---- geometric consistency filter (depthmap.cc:1320-1377) ----
  * depths[n] (n views, H*W each), poses R[n][9], t[n][3]; view `center` is
  * filtered against all others.  reproj_px > 0 adds a round-trip

@@ -72,6 +72,9 @@ struct pm_request {
     float *d0 = nullptr, *s0 = nullptr, *m1 = nullptr, *fdepth = nullptr, *fscore = nullptr;
     float *x_depth = nullptr, *x_score = nullptr, *x_plane3 = nullptr, *x_normal3 = nullptr;
     int32_t *x_best = nullptr;
+    float4 *seed = nullptr;              // seeding candidates from a prior result
+    unsigned long long *zbuf = nullptr;  // splat depth test of the prior warp
+    const pm_request *prior = nullptr;   // result reused as initialisation (may be null)
     double R[PM_MAX_SOURCES + 1][9] = {}, t[PM_MAX_SOURCES + 1][3] = {};
     bool have[PM_MAX_SOURCES + 1] = {};
     Trig trig;
@@ -202,6 +205,7 @@ void fill_args(pm_request *r) {
     a.col_trig = r->trig.col;
     a.ref = r->ref;
     a.plane = r->plane;
+    a.cand = r->seed;
     a.score = r->score;
     a.best = r->best;
     a.W = r->W;
@@ -286,8 +290,38 @@ int enqueue_post(pm_request *r) {
     return PM_OK;
 }
 
+// Splat the prior result into this keyframe and keep candidates that score
+// higher than the random initialisation.
+int enqueue_seed(pm_request *r, const pm_request *prior) {
+    pm::WarpArgs w{};
+    w.prev_plane = prior->plane;
+    w.prev_depth = prior->postprocessed ? prior->fdepth : nullptr;
+    if (!w.prev_depth) return fail(r->ctx, PM_EINVAL, "prior request has no post-filtered result");
+    w.Wp = prior->W;
+    w.Hp = prior->H;
+    w.prow = prior->trig.row;
+    w.pcol = prior->trig.col;
+    compose(prior->R[0], prior->t[0], r->R[0], r->t[0], w.M, w.c);
+    w.W = r->W;
+    w.H = r->H;
+    w.Wf = (float)r->W;
+    w.Hf = (float)r->H;
+    w.row = r->trig.row;
+    w.col = r->trig.col;
+    w.zbuf = r->zbuf;
+    w.seed = r->seed;
+    pm::launch_warp_prior(r->ctx->stream, w);
+    r->ctx->launches += 2;
+    for (int c = 0; c < 2; ++c) {
+        int rc = launch_tile(r, pm::kModeSeed, c, 0);
+        if (rc) return rc;
+    }
+    return PM_OK;
+}
+
 int enqueue_run(pm_request *r) {
     int rc = enqueue_init(r);
+    if (!rc && r->prior) rc = enqueue_seed(r, r->prior);
     if (!rc) rc = enqueue_sweeps(r, 0, 2 * r->prm.iterations);
     if (!rc && r->prm.postprocess) rc = enqueue_post(r);
     return rc;
@@ -473,6 +507,7 @@ size_t pm_request_bytes(int W, int H, int S, int fmt) {
     b += align256(N);                     // best
     b += 5 * align256(N * 4);             // d0 s0 m1 fdepth fscore
     b += 2 * align256(N * 4) + 2 * align256(N * 12) + align256(N * 4);  // export staging
+    b += align256(N * 16) + align256(N * 8);                            // seeding
     return b;
 }
 
@@ -525,6 +560,8 @@ int pm_request_create(pm_ctx *ctx, int W, int H, int S, const pm_params *params,
     r->x_plane3 = (float *)take(N * 12);
     r->x_normal3 = (float *)take(N * 12);
     r->x_best = (int32_t *)take(N * 4);
+    r->seed = (float4 *)take(N * 16);
+    r->zbuf = (unsigned long long *)take(N * 8);
     ctx->used += bytes;
     *out = r;
     return PM_OK;
@@ -633,6 +670,26 @@ int pm_request_sweep(pm_request *r, int first_half, int n_half) {
     return enqueue_sweeps(r, first_half, n_half);
 }
 
+int pm_request_set_prior(pm_request *r, const pm_request *prior) {
+    if (!r) return PM_EINVAL;
+    if (prior && prior->ctx != r->ctx) return fail(r->ctx, PM_EINVAL, "prior belongs to another context");
+    if (prior == r) return fail(r->ctx, PM_EINVAL, "a request cannot seed itself");
+    r->prior = prior;
+    r->graph_dirty = true;
+    return PM_OK;
+}
+
+int pm_request_seed(pm_request *r, const pm_request *prior) {
+    if (!r || !prior) return fail(r ? r->ctx : nullptr, PM_EINVAL, "NULL argument");
+    if (prior->ctx != r->ctx) return fail(r->ctx, PM_EINVAL, "prior belongs to another context");
+    int rc = check_views(r);
+    if (rc) return rc;
+    PM_CUDA(r->ctx, cudaSetDevice(r->ctx->device));
+    fill_args(r);
+    r->postprocessed = false;
+    return enqueue_seed(r, prior);
+}
+
 int pm_request_postprocess(pm_request *r) {
     if (!r) return PM_EINVAL;
     PM_CUDA(r->ctx, cudaSetDevice(r->ctx->device));
@@ -676,7 +733,7 @@ int pm_request_run(pm_request *r) {
         r->graph_dirty = false;
     }
     PM_CUDA(ctx, cudaGraphLaunch(r->gexec, ctx->stream));
-    ctx->launches += 3 + 2 * (uint64_t)r->prm.iterations + (r->prm.postprocess ? 3 : 0);
+    ctx->launches += 3 + 2 * (uint64_t)r->prm.iterations + (r->prm.postprocess ? 3 : 0) + (r->prior ? 4 : 0);
     r->postprocessed = r->prm.postprocess != 0;
     return PM_OK;
 }

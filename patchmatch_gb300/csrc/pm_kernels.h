@@ -26,6 +26,21 @@ cudaError_t dispatch_tile(int S, int fmt, dim3 grid, cudaStream_t st, const Swee
 cudaError_t dispatch_hyp(int S, int fmt, int n, cudaStream_t st, const HypArgs &a);
 dim3 tile_grid(int W, int H);
 
+// pm_seed.cu: prior result -> seeding candidates of a new keyframe
+struct WarpArgs {
+    const float4 *prev_plane;     // prior plane state (prior camera frame)
+    const float *prev_depth;      // prior filtered depth (0 = invalid)
+    int Wp, Hp;
+    const float2 *prow, *pcol;    // prior bearing tables
+    float M[9], c[3];             // prior camera -> new camera (FP64-composed)
+    int W, H;
+    float Wf, Hf;
+    const float2 *row, *col;      // new bearing tables
+    unsigned long long *zbuf;     // W*H scratch: (range bits, prior index) of the nearest splat
+    float4 *seed;                 // W*H candidates (w = range, 0 = none)
+};
+void launch_warp_prior(cudaStream_t st, const WarpArgs &a);
+
 // pm_post.cu
 struct PostArgs {
     const float4 *plane;

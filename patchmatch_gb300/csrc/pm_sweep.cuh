@@ -90,6 +90,11 @@ __global__ void __launch_bounds__(kThreads, tile_min_blocks<S>()) tile_kernel(co
     }
 
     const size_t idx = (size_t)i * W + j;
+    float4 cand = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (a.mode == kModeSeed) {
+        cand = a.cand[idx];
+        if (!(cand.w > 0.0f)) return;  // no candidate for this pixel
+    }
     const float4 cur = a.plane[idx];
     float score = a.score[idx];
     int best = a.best[idx];
@@ -99,13 +104,15 @@ __global__ void __launch_bounds__(kThreads, tile_min_blocks<S>()) tile_kernel(co
     float depth_hyp = 0.f;
     const float shift = Img::shift_for(Ic);
     const float halfW = 0.5f * a.Wf, halfH = 0.5f * a.Hf;
-    const int nh = a.mode == kModeScore ? 1 : 14;
+    const int nh = a.mode == kModeSweep ? 14 : 1;
 
 #pragma unroll 1
     for (int h = 0; h < nh; ++h) {
         float px, py, pz;
         if (a.mode == kModeScore) {
             px = hx; py = hy; pz = hz;
+        } else if (a.mode == kModeSeed) {
+            px = cand.x; py = cand.y; pz = cand.z;
         } else if (h < 8) {
             // neighbours (0,1),(1,0),(0,-1),(-1,0),(0,3),(3,0),(0,-3),(-3,0) (PatchMatchCuda.cu:305)
             const int sel = h & 3, far = (h >> 2) ? 3 : 1;
@@ -159,6 +166,10 @@ __global__ void __launch_bounds__(kThreads, tile_min_blocks<S>()) tile_kernel(co
         if (a.mode == kModeScore) {
             score = sc;
             best = hb;
+        } else if (a.mode == kModeSeed) {
+            if (sc > score) {  // the host seeding rule (depthmap.cc:483-487)
+                cx = px; cy = py; cz = pz; score = sc; current_depth = cand.w; best = hb;
+            }
         } else if (h < 8) {
             // smoothness weighting of propagated planes (PatchMatchCuda.cu:322-337)
             const float scale = __fadd_rn(__fadd_rn(__fmul_rn(px, bxc), __fmul_rn(py, byc)), __fmul_rn(pz, bzc));
@@ -182,6 +193,8 @@ __global__ void __launch_bounds__(kThreads, tile_min_blocks<S>()) tile_kernel(co
     if (a.mode == kModeSweep) {
         const float den = __fadd_rn(__fadd_rn(__fmul_rn(bxc, cx), __fmul_rn(byc, cy)), __fmul_rn(bzc, cz));
         a.plane[idx] = make_float4(cx, cy, cz, __fdiv_rn(1.0f, fmaxf(1e-6f, fabsf(den))));
+    } else if (a.mode == kModeSeed) {
+        a.plane[idx] = make_float4(cx, cy, cz, current_depth);
     }
 }
 

@@ -25,6 +25,7 @@ struct SweepArgs {
     const float2 *col_trig;     // W entries: (sin lon, cos lon)
     const float *ref;           // H x W reference intensities (float)
     float4 *plane;              // H x W: plane (x, y, z) and depth (w)
+    const float4 *cand;         // H x W seeding candidates (w = depth, 0 = none), mode kModeSeed
     float *score;               // H x W
     int8_t *best;               // H x W
     int W, H;
@@ -42,7 +43,9 @@ struct SweepArgs {
     float normal_range[6];      // refinement normal ranges 0.5 * 0.8^t
 };
 
-enum { kModeScore = 0, kModeSweep = 1 };
+// kModeScore: score each pixel's own plane; kModeSweep: red-black update;
+// kModeSeed: score the seeding candidate and keep it when it scores higher.
+enum { kModeScore = 0, kModeSweep = 1, kModeSeed = 2 };
 
 // Arguments of the fixed-hypothesis scoring kernel.
 struct HypArgs {

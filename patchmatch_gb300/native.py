@@ -25,6 +25,7 @@ EXPORTS = (
     "pm_stream", "pm_probe_fp32_peak",
     "pm_densify", "pm_request_create", "pm_request_destroy", "pm_request_bytes", "pm_request_set_params",
     "pm_request_set_view", "pm_request_init", "pm_request_set_state", "pm_request_sweep", "pm_request_postprocess",
+    "pm_request_seed", "pm_request_set_prior",
     "pm_request_run", "pm_request_read", "pm_request_synchronize", "pm_request_depth_device",
     "pm_score_hypotheses", "pm_filter_consistency", "pm_fuse", "pm_fuse_noalloc",
 )
@@ -82,6 +83,8 @@ def lib():
     L.pm_request_init.argtypes = [_vp]
     L.pm_request_set_state.argtypes = [_vp, _vp, _vp]
     L.pm_request_sweep.argtypes = [_vp, C.c_int, C.c_int]
+    L.pm_request_seed.argtypes = [_vp, _vp]
+    L.pm_request_set_prior.argtypes = [_vp, _vp]
     L.pm_request_postprocess.argtypes = [_vp]
     L.pm_request_run.argtypes = [_vp]
     L.pm_request_read.argtypes = [_vp, C.POINTER(Maps), C.c_int]
@@ -306,6 +309,13 @@ class Request:
 
     def sweep(self, first_half: int, n_half: int):
         self.ctx.check(self._L.pm_request_sweep(self.h, first_half, n_half))
+
+    def seed(self, prior: "Request"):
+        self.ctx.check(self._L.pm_request_seed(self.h, prior.h))
+
+    def set_prior(self, prior: "Request | None"):
+        self._prior = prior  # keep it alive
+        self.ctx.check(self._L.pm_request_set_prior(self.h, prior.h if prior is not None else None))
 
     def postprocess(self):
         self.ctx.check(self._L.pm_request_postprocess(self.h))

@@ -275,3 +275,63 @@ def test_odd_sizes_run(ctx):
     p = native.default_params(iterations=2)
     out = ctx.densify([v.gray_u8 for v in req.views], req.R, req.t, p)
     assert out["depth"].shape == (67, 131) and np.isfinite(out["depth"]).all()
+
+
+def test_prior_seeding_matches_oracle_and_speeds_convergence(ctx):
+    """Two keyframes along a path: B seeded from A's filtered result.  The
+    seeded state (init + seed, no sweeps) equals the oracle's choice wherever
+    the candidate and the random plane do not tie; a seeded run with 2 sweeps
+    is at least as accurate as an unseeded run with 8."""
+    sc = scene.Scene(scene.ROOM_OBJECTS, 51)
+    poses = [sc.trajectory_pose(7, 8, 10.0, t) for t in (1.0, 1.25, 1.5, 1.75)]
+    W, H = 512, 256
+    views = [sc.render(R, t, W, H) for R, t in poses]
+    imgs = [v.gray_u8 for v in views]
+    Rs = np.stack([v.R for v in views])
+    ts = np.stack([v.t for v in views])
+    # keyframe A = view 1 with sources 0, 2; keyframe B = view 2 with sources 1, 3
+    pa = native.default_params(iterations=8)
+    A = ctx.request(W, H, 2, pa)
+    A.set_views([imgs[1], imgs[0], imgs[2]], Rs[[1, 0, 2]], ts[[1, 0, 2]])
+    A.run()
+    a_out = A.read()
+    B = ctx.request(W, H, 2, native.default_params(iterations=0, postprocess=0, keyframe_id=1))
+    B.set_views([imgs[2], imgs[1], imgs[3]], Rs[[2, 1, 3]], ts[[2, 1, 3]])
+    B.init()
+    init = B.read(raw=True)
+    B.seed(A)
+    seeded = B.read(raw=True)
+    cand = O.warp_prior(a_out["plane"], a_out["depth"], Rs[1], ts[1], W, H, Rs[2], ts[2])
+    has = cand[..., 3] > 0
+    interior = np.zeros((H, W), bool)
+    interior[6:H - 5, 6:W - 5] = True
+    m = has & interior
+    ii, jj = np.nonzero(m)
+    V = O.Views(imgs[2].astype(np.float32), [imgs[1].astype(np.float32), imgs[3].astype(np.float32)],
+                Rs[[2, 1, 3]], ts[[2, 1, 3]])
+    cs, _ = O.cost_batch(V, O.cost_params(), np.stack([ii, jj], 1), cand[ii, jj, :3])
+    take = cs > init["score"][ii, jj]
+    expect = np.where(take[:, None], cand[ii, jj, :3], init["plane"][ii, jj])
+    got = seeded["plane"][ii, jj]
+    close = np.all(np.abs(got - expect) <= 1e-3 * np.abs(expect) + 1e-6, axis=1)
+    tie = np.abs(cs - init["score"][ii, jj]) < 1e-4
+    print(f"seeded pixels {m.mean():.3f}, taken {take.mean():.3f}, agreement {(close | tie).mean():.5f}")
+    assert (close | tie).mean() >= 0.995
+    # convergence: seeded + 2 sweeps vs unseeded 8 sweeps
+    gt = views[2].depth
+    def acc(d):
+        v = d > 0
+        return (np.abs(d[v] - gt[v]) / gt[v] < 0.01).mean(), v.mean()
+    B.set_params(native.default_params(iterations=2, keyframe_id=1))
+    B.set_prior(A)
+    B.run()
+    s2 = B.read()["depth"]
+    B.set_params(native.default_params(iterations=8, keyframe_id=1))
+    B.set_prior(None)
+    B.run()
+    u8 = B.read()["depth"]
+    (a_s, v_s), (a_u, v_u) = acc(s2), acc(u8)
+    print(f"seeded-2 acc1% {a_s:.4f} valid {v_s:.3f} | unseeded-8 acc1% {a_u:.4f} valid {v_u:.3f}")
+    assert a_s >= a_u - 0.02 and v_s >= v_u - 0.02
+    A.close()
+    B.close()
