@@ -106,6 +106,7 @@ typedef struct {
 
 typedef struct pm_ctx pm_ctx;
 typedef struct pm_request pm_request;
+typedef struct pm_result pm_result;
 
 /* Defaults of the reference path: patch_half 5, iterations 8, fold
  * combination, clamp seam, log-uniform/hemisphere init in [0.3, 20] m,
@@ -167,6 +168,17 @@ int pm_request_set_state(pm_request *req, const float *planes, const float *scor
  * into the new camera (the reference reuses them unrotated). */
 int pm_request_seed(pm_request *req, const pm_request *prior);
 int pm_request_set_prior(pm_request *req, const pm_request *prior);
+/* Retained results: a compact copy (plane state + filtered depth + pose,
+ * 20 bytes per pixel) of a finished request, kept for seeding later
+ * keyframes while the request itself is reused.  pm_result_snapshot enqueues
+ * the copy on the request's stream (the request must have been
+ * post-processed); pm_request_set_prior_result makes pm_request_run seed from
+ * it once the copy has finished.  The result must stay alive until then. */
+size_t pm_result_bytes(int width, int height);
+int pm_result_create(pm_ctx *ctx, int width, int height, pm_result **out);
+int pm_result_snapshot(pm_result *res, pm_request *req);
+int pm_result_destroy(pm_result *res);
+int pm_request_set_prior_result(pm_request *req, const pm_result *res);
 /* n_half red/black half-sweeps starting at half-sweep index first_half
  * (even = red, odd = black; sweep = first_half / 2).  Replaces
  * PatchMatchRedBlackPass (PatchMatchCuda.cu:568-615). */
@@ -175,9 +187,18 @@ int pm_request_sweep(pm_request *req, int first_half, int n_half);
 int pm_request_postprocess(pm_request *req);
 /* init + all sweeps + post-filter, replayed from a captured CUDA graph. */
 int pm_request_run(pm_request *req);
-/* Copy maps to the host (synchronous). raw = 1 returns the unfiltered sweep state. */
+/* Copy maps out (host or device destinations; synchronous).  raw = 1 returns
+ * the unfiltered sweep state.  _async enqueues the copies on the request's
+ * stream and returns; completion is visible through pm_request_query. */
 int pm_request_read(pm_request *req, pm_maps *out, int raw);
+int pm_request_read_async(pm_request *req, pm_maps *out, int raw);
 int pm_request_synchronize(pm_request *req);
+/* PM_OK when all work enqueued for the request has finished, PM_ENOTREADY
+ * while some is in flight. */
+int pm_request_query(const pm_request *req);
+/* The request's own CUDA stream (a cudaStream_t): every request runs on its
+ * own stream, so requests of one context overlap on the device. */
+void *pm_request_stream(const pm_request *req);
 /* Device pointer of the (filtered) depth map, H x W float, for chaining
  * into pm_filter/pm_fuse without a host round trip. */
 const float *pm_request_depth_device(const pm_request *req);
@@ -213,6 +234,53 @@ typedef struct {
  * Replaces DepthmapPruner::Prune (depthmap.cc:1535-1696). */
 int pm_fuse(pm_ctx *ctx, int width, int height, int n_views, float *const *depths, const double *R_cw,
             const double *t_cw, const uint8_t *bgr, float same_depth_threshold, float *pruned, pm_points *out);
+
+/* ---- served densification (a request loop over the calls above) ----
+ * Keyframes are submitted as SLAM emits them (any thread).  A worker thread
+ * owns the context: it admits keyframes in submission order as in-flight
+ * slots and the HBM budget allow, keeps every admitted keyframe's image
+ * resident on the device (a cache of cache_capacity keyframes) for reuse as a
+ * neighbour, selects as sources the nearest earlier keyframes whose camera
+ * baseline lies in [min_baseline, max_baseline] metres (min_sources ..
+ * max_sources of them), seeds each keyframe from the newest densified keyframe
+ * at least prior_lag submissions back (then runs seeded_iterations sweeps
+ * instead of params.iterations), and runs it on its own stream so keyframes
+ * that arrive while others are on the GPU overlap with them.  Every choice
+ * depends only on submission order, so a keyframe's result is the same
+ * whether it ran alone or among others.  Replaces the densification thread's
+ * loop (depthmap_computation_module.cc:205-472). */
+typedef struct pm_server pm_server;
+typedef struct {
+    pm_params params;        /* base parameters; params.iterations = sweeps without a prior */
+    int cache_capacity;      /* resident keyframes (40) */
+    int max_inflight;        /* keyframes on the GPU at once (4) */
+    int min_sources;         /* fewer earlier neighbours: the keyframe completes with PM_ENOTREADY */
+    int max_sources;
+    float min_baseline;      /* metres */
+    float max_baseline;
+    int seed_from_prior;     /* 1: reuse an earlier result as initialisation */
+    int seeded_iterations;   /* sweeps of a seeded keyframe (2) */
+    int prior_lag;           /* seed from the newest densified keyframe at least this many back (4) */
+    int poll_us;             /* worker polling interval while work is in flight */
+} pm_server_config;
+typedef struct {
+    int status;              /* PM_OK, PM_ENOTREADY (too few neighbours) or an error */
+    int n_sources;
+    int seeded;
+    int iterations;
+    double queue_ms;         /* submit -> start on the GPU */
+    double latency_ms;       /* submit -> maps on the host */
+} pm_served_info;
+void pm_server_config_default(pm_server_config *cfg);
+int pm_server_create(pm_ctx *ctx, const pm_server_config *cfg, pm_server **out);
+/* Copies the keyframe's gray image (uint8) and pose; returns a ticket. */
+int pm_server_submit(pm_server *srv, int width, int height, const pm_view *keyframe, uint64_t *ticket);
+/* Blocks until the ticket's keyframe is done (timeout_ms < 0: no limit;
+ * PM_ETIMEOUT otherwise), then fills out->depth / out->score (host, may be
+ * NULL) and info.  Returns the keyframe's status. */
+int pm_server_wait(pm_server *srv, uint64_t ticket, int timeout_ms, pm_maps *out, pm_served_info *info);
+/* Finishes all submitted keyframes, then releases everything. */
+int pm_server_destroy(pm_server *srv);
 
 /* ---- fusion for callers that cannot allocate device memory ----
  * Some callers must not allocate at the moment they fuse: a process whose

@@ -61,6 +61,27 @@ int pm_scene_render(const pm_scene *s, const double R[9], const double t[3], int
                     int supersample, float noise_sigma, uint32_t noise_seed, float *gray,
                     uint8_t *gray_u8, uint8_t *rgb, float *depth, float *normal);
 
+/* Plain description of a scene (for the device renderer). */
+#define PM_SCENE_MAX_BOXES 32
+#define PM_SCENE_MAX_CYLS 4
+typedef struct {
+    double room_lo[3], room_hi[3];
+    int n_boxes, n_cyls;
+    double box_lo[PM_SCENE_MAX_BOXES][3], box_hi[PM_SCENE_MAX_BOXES][3];
+    double cyl[PM_SCENE_MAX_CYLS][5]; /* cx, cz, r, y0, y1 */
+    uint32_t seed;
+    double base_freq;
+} pm_scene_desc;
+int pm_scene_describe(const pm_scene *s, pm_scene_desc *out);
+
+/* Render one view on the GPU into caller-owned device buffers (any may be
+ * NULL): gray_u8 H*W, depth H*W (range), bgr H*W*3.  Same scene, texture and
+ * conventions as pm_scene_render, evaluated in FP32; noise_sigma > 0 adds
+ * hashed Gaussian noise.  Enqueued on `stream` (a cudaStream_t). */
+int pm_scene_render_device(const pm_scene *s, const double R[9], const double t[3], int W, int H, int supersample,
+                           float noise_sigma, uint32_t noise_seed, uint8_t *gray_u8, float *depth, uint8_t *bgr,
+                           void *stream);
+
 #ifdef __cplusplus
 }
 #endif

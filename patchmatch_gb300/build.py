@@ -43,7 +43,7 @@ def _sources():
     deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     deps += [os.path.join(INC, f) for f in os.listdir(INC)]
     units = []
-    for f in ("pm_api.cu", "pm_prep.cu", "pm_post.cu", "pm_seed.cu", "pm_fuse_noalloc.cu", "pm_dense.cpp"):
+    for f in ("pm_api.cu", "pm_prep.cu", "pm_post.cu", "pm_seed.cu", "pm_fuse_noalloc.cu", "pm_dense.cpp", "pm_server.cpp"):
         units.append((os.path.join(CSRC, f), os.path.join(OBJ_DIR, os.path.splitext(f)[0] + ".o"), []))
     # the cost/sweep kernels flush subnormals to zero: no value on that path is
     # subnormal, and it keeps the approximate reciprocal/rsqrt/exp2 single
@@ -82,11 +82,19 @@ def build_pm(force: bool = False, jobs: int | None = None, verbose: bool = False
 
 
 def build_scene(force: bool = False) -> str:
+    """Host ray caster (g++/OpenMP) plus its device twin (nvcc), one library."""
     os.makedirs(LIB_DIR, exist_ok=True)
+    os.makedirs(OBJ_DIR, exist_ok=True)
     src = os.path.join(CSRC, "scene.cpp")
+    gsrc = os.path.join(CSRC, "scene_gpu.cu")
     lib = os.path.join(LIB_DIR, "libpm_scene.so")
-    if force or _stale(lib, [src, os.path.join(INC, "pm_scene.h")]):
-        _run(["g++", "-O2", "-fopenmp", "-fPIC", "-shared", "-std=c++17", "-I" + INC, "-o", lib, src])
+    deps = [src, gsrc, os.path.join(INC, "pm_scene.h")]
+    if force or _stale(lib, deps):
+        o1 = os.path.join(OBJ_DIR, "scene.o")
+        o2 = os.path.join(OBJ_DIR, "scene_gpu.o")
+        _run(["g++", "-O2", "-fopenmp", "-fPIC", "-std=c++17", "-I" + INC, "-c", src, "-o", o1])
+        _run([_nvcc()] + NVCC_FLAGS + ["-c", gsrc, "-o", o2])
+        _run([_nvcc(), "-shared"] + ARCH + ["-o", lib, o1, o2, "-Xcompiler", "-fopenmp"])
     return lib
 
 

@@ -75,14 +75,32 @@ struct pm_request {
     float4 *seed = nullptr;              // seeding candidates from a prior result
     unsigned long long *zbuf = nullptr;  // splat depth test of the prior warp
     const pm_request *prior = nullptr;   // result reused as initialisation (may be null)
+    const pm_result *prior_res = nullptr;
     double R[PM_MAX_SOURCES + 1][9] = {}, t[PM_MAX_SOURCES + 1][3] = {};
     bool have[PM_MAX_SOURCES + 1] = {};
     Trig trig;
     pm::SweepArgs args{};
+    cudaStream_t stream = nullptr;  // the request's own stream: requests overlap on the device
+    cudaEvent_t ready = nullptr;    // recorded on this stream for requests seeded from it
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
     bool graph_dirty = true;
     bool postprocessed = false;
+};
+
+// A retained keyframe result (plane state + filtered depth + pose): the
+// compact form in which results are kept for seeding later keyframes.
+struct pm_result {
+    pm_ctx *ctx = nullptr;
+    int W = 0, H = 0;
+    size_t bytes = 0;
+    void *block = nullptr;
+    float4 *plane = nullptr;
+    float *fdepth = nullptr;
+    double R[9] = {}, t[3] = {};
+    Trig trig;
+    cudaEvent_t ready = nullptr;  // recorded after the snapshot copies
+    bool valid = false;
 };
 
 namespace {
@@ -235,7 +253,7 @@ int launch_tile(pm_request *r, int mode, int colour, int sweep) {
     a.mode = mode;
     a.colour = colour;
     a.sweep = sweep;
-    cudaError_t e = pm::dispatch_tile(r->S, r->prm.image_format, pm::tile_grid(r->W, r->H), r->ctx->stream, a);
+    cudaError_t e = pm::dispatch_tile(r->S, r->prm.image_format, pm::tile_grid(r->W, r->H), r->stream, a);
     r->ctx->launches++;
     if (e != cudaSuccess) return fail(r->ctx, PM_ECUDA, "tile kernel launch: %s", cudaGetErrorString(e));
     return PM_OK;
@@ -249,7 +267,7 @@ int check_views(pm_request *r) {
 
 int enqueue_init(pm_request *r) {
     const pm_params &p = r->prm;
-    pm::launch_init_planes(r->ctx->stream, r->trig.row, r->trig.col, r->W, r->H, p.seed, p.keyframe_id, p.init_mode,
+    pm::launch_init_planes(r->stream, r->trig.row, r->trig.col, r->W, r->H, p.seed, p.keyframe_id, p.init_mode,
                            p.min_depth, p.max_depth, r->plane, r->score, r->best);
     r->ctx->launches++;
     for (int c = 0; c < 2; ++c) {
@@ -285,23 +303,31 @@ int enqueue_post(pm_request *r) {
     a.m1 = r->m1;
     a.out_depth = r->fdepth;
     a.out_score = r->fscore;
-    pm::launch_postprocess(r->ctx->stream, a);
+    pm::launch_postprocess(r->stream, a);
     r->ctx->launches += 3;
     return PM_OK;
 }
 
 // Splat the prior result into this keyframe and keep candidates that score
 // higher than the random initialisation.
-int enqueue_seed(pm_request *r, const pm_request *prior) {
+// Where a seeding prior comes from: a request's state or a retained result.
+struct PriorSrc {
+    const float4 *plane;
+    const float *fdepth;
+    int W, H;
+    Trig trig;
+    const double *R, *t;
+};
+
+int enqueue_seed_from(pm_request *r, const PriorSrc &prior) {
     pm::WarpArgs w{};
-    w.prev_plane = prior->plane;
-    w.prev_depth = prior->postprocessed ? prior->fdepth : nullptr;
-    if (!w.prev_depth) return fail(r->ctx, PM_EINVAL, "prior request has no post-filtered result");
-    w.Wp = prior->W;
-    w.Hp = prior->H;
-    w.prow = prior->trig.row;
-    w.pcol = prior->trig.col;
-    compose(prior->R[0], prior->t[0], r->R[0], r->t[0], w.M, w.c);
+    w.prev_plane = prior.plane;
+    w.prev_depth = prior.fdepth;
+    w.Wp = prior.W;
+    w.Hp = prior.H;
+    w.prow = prior.trig.row;
+    w.pcol = prior.trig.col;
+    compose(prior.R, prior.t, r->R[0], r->t[0], w.M, w.c);
     w.W = r->W;
     w.H = r->H;
     w.Wf = (float)r->W;
@@ -310,7 +336,7 @@ int enqueue_seed(pm_request *r, const pm_request *prior) {
     w.col = r->trig.col;
     w.zbuf = r->zbuf;
     w.seed = r->seed;
-    pm::launch_warp_prior(r->ctx->stream, w);
+    pm::launch_warp_prior(r->stream, w);
     r->ctx->launches += 2;
     for (int c = 0; c < 2; ++c) {
         int rc = launch_tile(r, pm::kModeSeed, c, 0);
@@ -319,9 +345,21 @@ int enqueue_seed(pm_request *r, const pm_request *prior) {
     return PM_OK;
 }
 
+int enqueue_seed(pm_request *r, const pm_request *prior) {
+    if (!prior->postprocessed) return fail(r->ctx, PM_EINVAL, "prior request has no post-filtered result");
+    return enqueue_seed_from(r, PriorSrc{prior->plane, prior->fdepth, prior->W, prior->H, prior->trig, prior->R[0],
+                                         prior->t[0]});
+}
+
+int enqueue_seed_result(pm_request *r, const pm_result *res) {
+    if (!res->valid) return fail(r->ctx, PM_EINVAL, "prior result holds no snapshot");
+    return enqueue_seed_from(r, PriorSrc{res->plane, res->fdepth, res->W, res->H, res->trig, res->R, res->t});
+}
+
 int enqueue_run(pm_request *r) {
     int rc = enqueue_init(r);
     if (!rc && r->prior) rc = enqueue_seed(r, r->prior);
+    else if (!rc && r->prior_res) rc = enqueue_seed_result(r, r->prior_res);
     if (!rc) rc = enqueue_sweeps(r, 0, 2 * r->prm.iterations);
     if (!rc && r->prm.postprocess) rc = enqueue_post(r);
     return rc;
@@ -539,6 +577,14 @@ int pm_request_create(pm_ctx *ctx, int W, int H, int S, const pm_params *params,
         delete r;
         return fail(ctx, PM_ENOMEM, "device allocation of %zu bytes failed", bytes);
     }
+    if (cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&r->ready, cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError();
+        if (r->stream) cudaStreamDestroy(r->stream);
+        cudaFree(r->block);
+        delete r;
+        return fail(ctx, PM_ECUDA, "stream creation failed");
+    }
     const size_t N = (size_t)W * H, NQ = (size_t)(W + 1) * (H + 1);
     const size_t qb = params->image_format == PM_IMAGE_F16 ? 8 : 4;
     char *p = static_cast<char *>(r->block);
@@ -571,9 +617,11 @@ int pm_request_destroy(pm_request *r) {
     if (!r) return PM_EINVAL;
     pm_ctx *ctx = r->ctx;
     cudaSetDevice(ctx->device);
-    cudaStreamSynchronize(ctx->stream);
+    cudaStreamSynchronize(r->stream);
     if (r->gexec) cudaGraphExecDestroy(r->gexec);
     if (r->graph) cudaGraphDestroy(r->graph);
+    cudaEventDestroy(r->ready);
+    cudaStreamDestroy(r->stream);
     cudaFree(r->block);
     ctx->used -= r->bytes;
     if (ctx->cached == r) ctx->cached = nullptr;
@@ -604,15 +652,15 @@ int pm_request_set_view(pm_request *r, int k, const pm_view *v) {
     const size_t row = (size_t)r->W * es;
     const size_t pitch = v->pitch_bytes ? v->pitch_bytes : row;
     if (pitch < row) return fail(ctx, PM_EINVAL, "pitch %zu smaller than a row (%zu)", pitch, row);
-    PM_CUDA(ctx, cudaMemcpy2DAsync(r->raw, row, v->gray, pitch, row, r->H, cudaMemcpyHostToDevice, ctx->stream));
+    PM_CUDA(ctx, cudaMemcpy2DAsync(r->raw, row, v->gray, pitch, row, r->H, cudaMemcpyDefault, r->stream));
     if (k == 0) {
-        pm::launch_ref_to_float(ctx->stream, r->raw, row, r->prm.image_format, r->W, r->H, r->ref);
+        pm::launch_ref_to_float(r->stream, r->raw, row, r->prm.image_format, r->W, r->H, r->ref);
         ctx->launches++;
         r->has_mask = v->mask != nullptr;
         if (v->mask)
-            PM_CUDA(ctx, cudaMemcpyAsync(r->mask, v->mask, (size_t)r->W * r->H, cudaMemcpyHostToDevice, ctx->stream));
+            PM_CUDA(ctx, cudaMemcpyAsync(r->mask, v->mask, (size_t)r->W * r->H, cudaMemcpyDefault, r->stream));
     } else {
-        pm::launch_build_quad(ctx->stream, r->raw, row, r->prm.image_format, r->W, r->H, r->prm.seam, r->quad[k - 1]);
+        pm::launch_build_quad(r->stream, r->raw, row, r->prm.image_format, r->W, r->H, r->prm.seam, r->quad[k - 1]);
         ctx->launches++;
     }
     PM_CUDA(ctx, cudaGetLastError());
@@ -644,9 +692,9 @@ int pm_request_set_state(pm_request *r, const float *planes, const float *scores
     rc = ensure_scratch(ctx, N * 16);
     if (rc) return rc;
     float *dpl = (float *)ctx->scratch, *dsc = dpl + 3 * N;
-    PM_CUDA(ctx, cudaMemcpyAsync(dpl, planes, N * 12, cudaMemcpyHostToDevice, ctx->stream));
-    if (scores) PM_CUDA(ctx, cudaMemcpyAsync(dsc, scores, N * 4, cudaMemcpyHostToDevice, ctx->stream));
-    pm::launch_set_planes(ctx->stream, dpl, scores ? dsc : nullptr, r->trig.row, r->trig.col, r->W, r->H, r->plane,
+    PM_CUDA(ctx, cudaMemcpyAsync(dpl, planes, N * 12, cudaMemcpyHostToDevice, r->stream));
+    if (scores) PM_CUDA(ctx, cudaMemcpyAsync(dsc, scores, N * 4, cudaMemcpyHostToDevice, r->stream));
+    pm::launch_set_planes(r->stream, dpl, scores ? dsc : nullptr, r->trig.row, r->trig.col, r->W, r->H, r->plane,
                           r->score, r->best);
     ctx->launches++;
     if (!scores)
@@ -654,7 +702,7 @@ int pm_request_set_state(pm_request *r, const float *planes, const float *scores
             rc = launch_tile(r, pm::kModeScore, c, 0);
             if (rc) return rc;
         }
-    PM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    PM_CUDA(ctx, cudaStreamSynchronize(r->stream));
     r->postprocessed = false;
     return PM_OK;
 }
@@ -670,12 +718,94 @@ int pm_request_sweep(pm_request *r, int first_half, int n_half) {
     return enqueue_sweeps(r, first_half, n_half);
 }
 
+// Order this request's stream after all work enqueued so far on the prior's.
+static int wait_for_prior(pm_request *r, const pm_request *prior) {
+    if (!prior || prior->stream == r->stream) return PM_OK;
+    PM_CUDA(r->ctx, cudaEventRecord(prior->ready, prior->stream));
+    PM_CUDA(r->ctx, cudaStreamWaitEvent(r->stream, prior->ready, 0));
+    return PM_OK;
+}
+
 int pm_request_set_prior(pm_request *r, const pm_request *prior) {
     if (!r) return PM_EINVAL;
     if (prior && prior->ctx != r->ctx) return fail(r->ctx, PM_EINVAL, "prior belongs to another context");
     if (prior == r) return fail(r->ctx, PM_EINVAL, "a request cannot seed itself");
     r->prior = prior;
+    r->prior_res = nullptr;
     r->graph_dirty = true;
+    return PM_OK;
+}
+
+int pm_request_set_prior_result(pm_request *r, const pm_result *res) {
+    if (!r) return PM_EINVAL;
+    if (res && res->ctx != r->ctx) return fail(r->ctx, PM_EINVAL, "result belongs to another context");
+    r->prior_res = res;
+    r->prior = nullptr;
+    r->graph_dirty = true;
+    return PM_OK;
+}
+
+size_t pm_result_bytes(int W, int H) { return align256((size_t)W * H * 16) + align256((size_t)W * H * 4); }
+
+int pm_result_create(pm_ctx *ctx, int W, int H, pm_result **out) {
+    if (!ctx || !out) return fail(ctx, PM_EINVAL, "NULL argument");
+    *out = nullptr;
+    int rc = validate_size(ctx, W, H, 1);
+    if (rc) return rc;
+    PM_CUDA(ctx, cudaSetDevice(ctx->device));
+    const size_t bytes = pm_result_bytes(W, H);
+    if (ctx->used + bytes > ctx->budget)
+        return fail(ctx, PM_EBUDGET, "result needs %zu bytes, %zu of %zu in use", bytes, ctx->used, ctx->budget);
+    pm_result *r = new pm_result();
+    r->ctx = ctx;
+    r->W = W;
+    r->H = H;
+    r->bytes = bytes;
+    rc = get_trig(ctx, W, H, &r->trig);
+    if (!rc && cudaMalloc(&r->block, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        rc = fail(ctx, PM_ENOMEM, "device allocation of %zu bytes failed", bytes);
+    }
+    if (!rc && cudaEventCreateWithFlags(&r->ready, cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(r->block);
+        rc = fail(ctx, PM_ECUDA, "event creation failed");
+    }
+    if (rc) {
+        delete r;
+        return rc;
+    }
+    r->plane = (float4 *)r->block;
+    r->fdepth = (float *)((char *)r->block + align256((size_t)W * H * 16));
+    ctx->used += bytes;
+    *out = r;
+    return PM_OK;
+}
+
+int pm_result_snapshot(pm_result *res, pm_request *r) {
+    if (!res || !r) return PM_EINVAL;
+    if (res->ctx != r->ctx || res->W != r->W || res->H != r->H)
+        return fail(r->ctx, PM_EINVAL, "result and request differ in context or size");
+    if (!r->postprocessed) return fail(r->ctx, PM_EINVAL, "request has no post-filtered result");
+    PM_CUDA(r->ctx, cudaSetDevice(r->ctx->device));
+    const size_t N = (size_t)r->W * r->H;
+    PM_CUDA(r->ctx, cudaMemcpyAsync(res->plane, r->plane, N * 16, cudaMemcpyDeviceToDevice, r->stream));
+    PM_CUDA(r->ctx, cudaMemcpyAsync(res->fdepth, r->fdepth, N * 4, cudaMemcpyDeviceToDevice, r->stream));
+    PM_CUDA(r->ctx, cudaEventRecord(res->ready, r->stream));
+    std::memcpy(res->R, r->R[0], sizeof res->R);
+    std::memcpy(res->t, r->t[0], sizeof res->t);
+    res->valid = true;
+    return PM_OK;
+}
+
+int pm_result_destroy(pm_result *res) {
+    if (!res) return PM_EINVAL;
+    cudaSetDevice(res->ctx->device);
+    cudaEventSynchronize(res->ready);
+    cudaEventDestroy(res->ready);
+    cudaFree(res->block);
+    res->ctx->used -= res->bytes;
+    delete res;
     return PM_OK;
 }
 
@@ -687,6 +817,8 @@ int pm_request_seed(pm_request *r, const pm_request *prior) {
     PM_CUDA(r->ctx, cudaSetDevice(r->ctx->device));
     fill_args(r);
     r->postprocessed = false;
+    rc = wait_for_prior(r, prior);
+    if (rc) return rc;
     return enqueue_seed(r, prior);
 }
 
@@ -707,10 +839,10 @@ int pm_request_run(pm_request *r) {
     if (r->graph_dirty || !r->gexec) {
         fill_args(r);
         cudaGraph_t g = nullptr;
-        PM_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        PM_CUDA(ctx, cudaStreamBeginCapture(r->stream, cudaStreamCaptureModeThreadLocal));
         const uint64_t before = ctx->launches;
         rc = enqueue_run(r);
-        cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);
+        cudaError_t ce = cudaStreamEndCapture(r->stream, &g);
         if (rc) {
             if (g) cudaGraphDestroy(g);
             return rc;
@@ -732,39 +864,61 @@ int pm_request_run(pm_request *r) {
         r->graph = g;
         r->graph_dirty = false;
     }
-    PM_CUDA(ctx, cudaGraphLaunch(r->gexec, ctx->stream));
-    ctx->launches += 3 + 2 * (uint64_t)r->prm.iterations + (r->prm.postprocess ? 3 : 0) + (r->prior ? 4 : 0);
+    rc = wait_for_prior(r, r->prior);
+    if (rc) return rc;
+    if (r->prior_res) PM_CUDA(ctx, cudaStreamWaitEvent(r->stream, r->prior_res->ready, 0));
+    PM_CUDA(ctx, cudaGraphLaunch(r->gexec, r->stream));
+    ctx->launches += 3 + 2 * (uint64_t)r->prm.iterations + (r->prm.postprocess ? 3 : 0) +
+                     ((r->prior || r->prior_res) ? 4 : 0);
     r->postprocessed = r->prm.postprocess != 0;
     return PM_OK;
 }
 
-int pm_request_read(pm_request *r, pm_maps *out, int raw) {
+static int enqueue_read(pm_request *r, pm_maps *out, int raw) {
     if (!r || !out) return fail(r ? r->ctx : nullptr, PM_EINVAL, "NULL argument");
     pm_ctx *ctx = r->ctx;
     PM_CUDA(ctx, cudaSetDevice(ctx->device));
     const size_t N = (size_t)r->W * r->H;
     const int use_raw = raw || !r->postprocessed;
-    pm::launch_export(ctx->stream, r->plane, r->score, r->best, r->fdepth, r->fscore, r->trig.row, r->trig.col, r->W,
+    pm::launch_export(r->stream, r->plane, r->score, r->best, r->fdepth, r->fscore, r->trig.row, r->trig.col, r->W,
                       r->H, use_raw, r->x_depth, r->x_score, r->x_plane3, r->x_normal3, r->x_best);
     ctx->launches++;
-    if (out->depth) PM_CUDA(ctx, cudaMemcpyAsync(out->depth, r->x_depth, N * 4, cudaMemcpyDeviceToHost, ctx->stream));
-    if (out->score) PM_CUDA(ctx, cudaMemcpyAsync(out->score, r->x_score, N * 4, cudaMemcpyDeviceToHost, ctx->stream));
-    if (out->plane) PM_CUDA(ctx, cudaMemcpyAsync(out->plane, r->x_plane3, N * 12, cudaMemcpyDeviceToHost, ctx->stream));
-    if (out->normal)
-        PM_CUDA(ctx, cudaMemcpyAsync(out->normal, r->x_normal3, N * 12, cudaMemcpyDeviceToHost, ctx->stream));
+    // host or device destinations
+    if (out->depth) PM_CUDA(ctx, cudaMemcpyAsync(out->depth, r->x_depth, N * 4, cudaMemcpyDefault, r->stream));
+    if (out->score) PM_CUDA(ctx, cudaMemcpyAsync(out->score, r->x_score, N * 4, cudaMemcpyDefault, r->stream));
+    if (out->plane) PM_CUDA(ctx, cudaMemcpyAsync(out->plane, r->x_plane3, N * 12, cudaMemcpyDefault, r->stream));
+    if (out->normal) PM_CUDA(ctx, cudaMemcpyAsync(out->normal, r->x_normal3, N * 12, cudaMemcpyDefault, r->stream));
     if (out->best_view)
-        PM_CUDA(ctx, cudaMemcpyAsync(out->best_view, r->x_best, N * 4, cudaMemcpyDeviceToHost, ctx->stream));
-    PM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        PM_CUDA(ctx, cudaMemcpyAsync(out->best_view, r->x_best, N * 4, cudaMemcpyDefault, r->stream));
     return PM_OK;
 }
 
+int pm_request_read(pm_request *r, pm_maps *out, int raw) {
+    int rc = enqueue_read(r, out, raw);
+    if (rc) return rc;
+    PM_CUDA(r->ctx, cudaStreamSynchronize(r->stream));
+    return PM_OK;
+}
+
+int pm_request_read_async(pm_request *r, pm_maps *out, int raw) { return enqueue_read(r, out, raw); }
+
 int pm_request_synchronize(pm_request *r) {
     if (!r) return PM_EINVAL;
-    PM_CUDA(r->ctx, cudaStreamSynchronize(r->ctx->stream));
+    PM_CUDA(r->ctx, cudaStreamSynchronize(r->stream));
     return PM_OK;
 }
 
 const float *pm_request_depth_device(const pm_request *r) { return r ? r->fdepth : nullptr; }
+
+void *pm_request_stream(const pm_request *r) { return r ? (void *)r->stream : nullptr; }
+
+int pm_request_query(const pm_request *r) {
+    if (!r) return PM_EINVAL;
+    const cudaError_t e = cudaStreamQuery(r->stream);
+    if (e == cudaSuccess) return PM_OK;
+    if (e == cudaErrorNotReady) return PM_ENOTREADY;
+    return PM_ECUDA;
+}
 
 int pm_densify(pm_ctx *ctx, int W, int H, const pm_view *views, int n_views, const pm_params *params, pm_maps *out) {
     if (!ctx || !views || !out || !out->depth) return fail(ctx, PM_EINVAL, "NULL argument");
@@ -821,8 +975,8 @@ int pm_score_hypotheses(pm_request *r, int n, const int32_t *ij, const float *pl
     int *dbest = (int *)p;
     p += align256((size_t)n * 4);
     float *dper = (float *)p;
-    PM_CUDA(ctx, cudaMemcpyAsync(dij, ij, (size_t)n * 8, cudaMemcpyHostToDevice, ctx->stream));
-    PM_CUDA(ctx, cudaMemcpyAsync(dpl, planes, (size_t)n * 12, cudaMemcpyHostToDevice, ctx->stream));
+    PM_CUDA(ctx, cudaMemcpyAsync(dij, ij, (size_t)n * 8, cudaMemcpyHostToDevice, r->stream));
+    PM_CUDA(ctx, cudaMemcpyAsync(dpl, planes, (size_t)n * 12, cudaMemcpyHostToDevice, r->stream));
     pm::HypArgs a{};
     a.P = r->args.P;
     for (int k = 0; k < r->S; ++k) a.quad[k] = r->quad[k];
@@ -847,14 +1001,14 @@ int pm_score_hypotheses(pm_request *r, int n, const int32_t *ij, const float *pl
     a.scores = dsc;
     a.best = dbest;
     a.per_source = per_source ? dper : nullptr;
-    cudaError_t e = pm::dispatch_hyp(r->S, r->prm.image_format, n, ctx->stream, a);
+    cudaError_t e = pm::dispatch_hyp(r->S, r->prm.image_format, n, r->stream, a);
     ctx->launches++;
     if (e != cudaSuccess) return fail(ctx, PM_ECUDA, "hypothesis kernel: %s", cudaGetErrorString(e));
-    if (scores) PM_CUDA(ctx, cudaMemcpyAsync(scores, dsc, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
-    if (best) PM_CUDA(ctx, cudaMemcpyAsync(best, dbest, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    if (scores) PM_CUDA(ctx, cudaMemcpyAsync(scores, dsc, (size_t)n * 4, cudaMemcpyDeviceToHost, r->stream));
+    if (best) PM_CUDA(ctx, cudaMemcpyAsync(best, dbest, (size_t)n * 4, cudaMemcpyDeviceToHost, r->stream));
     if (per_source)
-        PM_CUDA(ctx, cudaMemcpyAsync(per_source, dper, (size_t)n * 4 * S, cudaMemcpyDeviceToHost, ctx->stream));
-    PM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        PM_CUDA(ctx, cudaMemcpyAsync(per_source, dper, (size_t)n * 4 * S, cudaMemcpyDeviceToHost, r->stream));
+    PM_CUDA(ctx, cudaStreamSynchronize(r->stream));
     return PM_OK;
 }
 

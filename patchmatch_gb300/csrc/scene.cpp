@@ -226,6 +226,29 @@ pm_scene *pm_scene_create(int kind, uint32_t seed) {
 
 void pm_scene_destroy(pm_scene *s) { delete s; }
 
+int pm_scene_describe(const pm_scene *s, pm_scene_desc *out) {
+    if (!s || !out) return 1;
+    std::memset(out, 0, sizeof *out);
+    for (int a = 0; a < 3; ++a) {
+        out->room_lo[a] = s->room.lo[a];
+        out->room_hi[a] = s->room.hi[a];
+    }
+    out->n_boxes = std::min((int)s->boxes.size(), PM_SCENE_MAX_BOXES);
+    for (int k = 0; k < out->n_boxes; ++k)
+        for (int a = 0; a < 3; ++a) {
+            out->box_lo[k][a] = s->boxes[k].lo[a];
+            out->box_hi[k][a] = s->boxes[k].hi[a];
+        }
+    out->n_cyls = std::min((int)s->cyls.size(), PM_SCENE_MAX_CYLS);
+    for (int k = 0; k < out->n_cyls; ++k) {
+        const Cyl &c = s->cyls[k];
+        out->cyl[k][0] = c.cx; out->cyl[k][1] = c.cz; out->cyl[k][2] = c.r; out->cyl[k][3] = c.y0; out->cyl[k][4] = c.y1;
+    }
+    out->seed = s->seed;
+    out->base_freq = s->base_freq;
+    return 0;
+}
+
 int pm_scene_poses(const pm_scene *s, int n_views, uint32_t seed, float bmin, float bmax, float yaw_deg,
                    double *R, double *t) {
     if (!s || n_views < 1 || !R || !t) return 1;

@@ -25,9 +25,12 @@ EXPORTS = (
     "pm_stream", "pm_probe_fp32_peak",
     "pm_densify", "pm_request_create", "pm_request_destroy", "pm_request_bytes", "pm_request_set_params",
     "pm_request_set_view", "pm_request_init", "pm_request_set_state", "pm_request_sweep", "pm_request_postprocess",
-    "pm_request_seed", "pm_request_set_prior",
-    "pm_request_run", "pm_request_read", "pm_request_synchronize", "pm_request_depth_device",
+    "pm_request_seed", "pm_request_set_prior", "pm_result_bytes", "pm_result_create", "pm_result_snapshot",
+    "pm_result_destroy", "pm_request_set_prior_result",
+    "pm_request_run", "pm_request_read", "pm_request_read_async", "pm_request_synchronize", "pm_request_query",
+    "pm_request_stream", "pm_request_depth_device",
     "pm_score_hypotheses", "pm_filter_consistency", "pm_fuse", "pm_fuse_noalloc",
+    "pm_server_config_default", "pm_server_create", "pm_server_submit", "pm_server_wait", "pm_server_destroy",
 )
 
 
@@ -52,6 +55,18 @@ class Maps(C.Structure):
 class Points(C.Structure):
     _fields_ = [("capacity", C.c_int), ("count", C.c_int), ("xyz", C.c_void_p), ("bgr", C.c_void_p),
                 ("ij", C.c_void_p)]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("params", Params), ("cache_capacity", C.c_int), ("max_inflight", C.c_int),
+                ("min_sources", C.c_int), ("max_sources", C.c_int), ("min_baseline", C.c_float),
+                ("max_baseline", C.c_float), ("seed_from_prior", C.c_int), ("seeded_iterations", C.c_int),
+                ("prior_lag", C.c_int), ("poll_us", C.c_int)]
+
+
+class ServedInfo(C.Structure):
+    _fields_ = [("status", C.c_int), ("n_sources", C.c_int), ("seeded", C.c_int), ("iterations", C.c_int),
+                ("queue_ms", C.c_double), ("latency_ms", C.c_double)]
 
 
 _vp, _sz = C.c_void_p, C.c_size_t
@@ -84,11 +99,21 @@ def lib():
     L.pm_request_set_state.argtypes = [_vp, _vp, _vp]
     L.pm_request_sweep.argtypes = [_vp, C.c_int, C.c_int]
     L.pm_request_seed.argtypes = [_vp, _vp]
+    L.pm_result_bytes.restype = _sz
+    L.pm_result_bytes.argtypes = [C.c_int, C.c_int]
+    L.pm_result_create.argtypes = [_vp, C.c_int, C.c_int, C.POINTER(_vp)]
+    L.pm_result_snapshot.argtypes = [_vp, _vp]
+    L.pm_result_destroy.argtypes = [_vp]
+    L.pm_request_set_prior_result.argtypes = [_vp, _vp]
     L.pm_request_set_prior.argtypes = [_vp, _vp]
     L.pm_request_postprocess.argtypes = [_vp]
     L.pm_request_run.argtypes = [_vp]
     L.pm_request_read.argtypes = [_vp, C.POINTER(Maps), C.c_int]
     L.pm_request_synchronize.argtypes = [_vp]
+    L.pm_request_read_async.argtypes = [_vp, C.POINTER(Maps), C.c_int]
+    L.pm_request_query.argtypes = [_vp]
+    L.pm_request_stream.restype = _vp
+    L.pm_request_stream.argtypes = [_vp]
     L.pm_request_depth_device.restype = _vp
     L.pm_request_depth_device.argtypes = [_vp]
     L.pm_score_hypotheses.argtypes = [_vp, C.c_int, _vp, _vp, _vp, _vp, _vp]
@@ -97,6 +122,11 @@ def lib():
     L.pm_fuse.argtypes = [_vp, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, C.c_float, _vp, C.POINTER(Points)]
     L.pm_fuse_noalloc.argtypes = [C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, C.c_float, _vp, _vp, _vp, _vp, _vp,
                                   _vp]
+    L.pm_server_config_default.argtypes = [C.POINTER(ServerConfig)]
+    L.pm_server_create.argtypes = [_vp, C.POINTER(ServerConfig), C.POINTER(_vp)]
+    L.pm_server_submit.argtypes = [_vp, C.c_int, C.c_int, C.POINTER(View), C.POINTER(C.c_uint64)]
+    L.pm_server_wait.argtypes = [_vp, C.c_uint64, C.c_int, C.POINTER(Maps), C.POINTER(ServedInfo)]
+    L.pm_server_destroy.argtypes = [_vp]
     L._pm_typed = True
     return L
 
@@ -313,9 +343,12 @@ class Request:
     def seed(self, prior: "Request"):
         self.ctx.check(self._L.pm_request_seed(self.h, prior.h))
 
-    def set_prior(self, prior: "Request | None"):
+    def set_prior(self, prior: "Request | Result | None"):
         self._prior = prior  # keep it alive
-        self.ctx.check(self._L.pm_request_set_prior(self.h, prior.h if prior is not None else None))
+        if isinstance(prior, Result):
+            self.ctx.check(self._L.pm_request_set_prior_result(self.h, prior.h))
+        else:
+            self.ctx.check(self._L.pm_request_set_prior(self.h, prior.h if prior is not None else None))
 
     def postprocess(self):
         self.ctx.check(self._L.pm_request_postprocess(self.h))
@@ -325,6 +358,18 @@ class Request:
 
     def synchronize(self):
         self.ctx.check(self._L.pm_request_synchronize(self.h))
+
+    @property
+    def stream_handle(self) -> int:
+        """cudaStream_t of the request (for torch.cuda.ExternalStream)."""
+        return int(self._L.pm_request_stream(self.h))
+
+    def done(self) -> bool:
+        rc = self._L.pm_request_query(self.h)
+        if rc == PM_ENOTREADY:
+            return False
+        self.ctx.check(rc)
+        return True
 
     def read(self, raw: bool = False, want=("depth", "score", "plane", "normal", "best_view")):
         out, maps = _alloc_maps(self.H, self.W, want)
@@ -341,3 +386,90 @@ class Request:
         self.ctx.check(self._L.pm_score_hypotheses(self.h, n, _ptr(ij), _ptr(planes), _ptr(scores), _ptr(best),
                                                    _ptr(ps)))
         return (scores, best, ps) if per_source else (scores, best)
+
+
+class Result:
+    """A retained keyframe result (pm_result): plane state + filtered depth + pose."""
+
+    def __init__(self, ctx: Context, W: int, H: int):
+        self.ctx, self.W, self.H = ctx, W, H
+        self._L = ctx._L
+        h = C.c_void_p()
+        ctx.check(self._L.pm_result_create(ctx.h, W, H, C.byref(h)))
+        self.h = h.value
+
+    def snapshot(self, req: Request):
+        self.ctx.check(self._L.pm_result_snapshot(self.h, req.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._L.pm_result_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def server_config(**kw) -> ServerConfig:
+    """Defaults of pm_server_config_default; keyword overrides, params=... for pm_params."""
+    c = ServerConfig()
+    lib().pm_server_config_default(C.byref(c))
+    for k, v in kw.items():
+        if not hasattr(c, k):
+            raise AttributeError(k)
+        setattr(c, k, v)
+    return c
+
+
+class Server:
+    """The served request loop (pm_server) on one context."""
+
+    def __init__(self, ctx: Context, cfg: ServerConfig | None = None):
+        self.ctx = ctx
+        self._L = ctx._L
+        self.cfg = cfg or server_config()
+        h = C.c_void_p()
+        rc = self._L.pm_server_create(ctx.h, C.byref(self.cfg), C.byref(h))
+        if rc != PM_OK:
+            raise PmError(rc, "pm_server_create failed")
+        self.h = h.value
+        self.shape = {}
+
+    def submit(self, gray, R, t) -> int:
+        gray = np.ascontiguousarray(gray, np.uint8)
+        H, W = gray.shape
+        v = make_view(gray, R, t)
+        tk = C.c_uint64()
+        rc = self._L.pm_server_submit(self.h, W, H, C.byref(v), C.byref(tk))
+        if rc != PM_OK:
+            raise PmError(rc, "pm_server_submit failed")
+        self.shape[tk.value] = (H, W)
+        return tk.value
+
+    def wait(self, ticket: int, timeout_ms: int = -1, want_score: bool = False):
+        """Returns (status, depth or None, score or None, info dict)."""
+        H, W = self.shape.pop(ticket)
+        depth = np.zeros((H, W), np.float32)
+        score = np.zeros((H, W), np.float32) if want_score else None
+        m = Maps()
+        m.depth = depth.ctypes.data
+        m.score = score.ctypes.data if want_score else None
+        info = ServedInfo()
+        rc = self._L.pm_server_wait(self.h, ticket, timeout_ms, C.byref(m), C.byref(info))
+        d = {k: getattr(info, k) for k, _ in ServedInfo._fields_}
+        ok = rc == PM_OK
+        return rc, (depth if ok else None), (score if ok else None), d
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._L.pm_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -33,6 +33,9 @@ def _lib():
         lib.pm_scene_trajectory_pose.restype = C.c_int
         lib.pm_scene_trajectory_pose.argtypes = [C.c_void_p, C.c_uint32, C.c_int, C.c_double,
                                                  C.c_double, _dp, _dp]
+        lib.pm_scene_render_device.restype = C.c_int
+        lib.pm_scene_render_device.argtypes = [C.c_void_p, _dp, _dp, C.c_int, C.c_int, C.c_int, C.c_float,
+                                               C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         lib.pm_scene_render.restype = C.c_int
         lib.pm_scene_render.argtypes = [C.c_void_p, _dp, _dp, C.c_int, C.c_int, C.c_int, C.c_float,
                                         C.c_uint32, _fp, _u8p, _u8p, _fp, _fp]
@@ -86,6 +89,17 @@ class Scene:
         if rc:
             raise RuntimeError("pm_scene_trajectory_pose failed")
         return R, t
+
+    def render_device(self, R, t, W: int, H: int, gray=None, depth=None, bgr=None, supersample: int = 2,
+                      noise_sigma: float = 0.0, noise_seed: int = 0, stream: int = 0):
+        """Render on the GPU into torch CUDA tensors (uint8 (H, W), float32 (H, W), uint8 (H, W, 3))."""
+        R = np.ascontiguousarray(R, np.float64)
+        t = np.ascontiguousarray(t, np.float64)
+        p = lambda x: None if x is None else x.data_ptr()
+        rc = self._lib.pm_scene_render_device(self._h, _ptr(R, _dp), _ptr(t, _dp), W, H, supersample, noise_sigma,
+                                              noise_seed, p(gray), p(depth), p(bgr), stream)
+        if rc:
+            raise RuntimeError("pm_scene_render_device failed")
 
     def render(self, R, t, W: int, H: int, supersample: int = 2, noise_sigma: float = 0.0,
                noise_seed: int = 0) -> View:
@@ -150,3 +164,50 @@ def config_request(cfg: int, seed: int = 0, W: int | None = None, H: int | None 
     if cfg == 3:
         return make_request(ROOM, W or 3840, H or 1920, n_src or 8, seed, 0.2, 0.5, 15.0, noise_sigma=2.0)
     raise ValueError(f"unknown workload {cfg}")
+
+
+@dataclass
+class Keyframe:
+    """One keyframe of a served stream: arrival time, image, pose, ground truth."""
+    t_s: float
+    gray_u8: np.ndarray
+    depth: np.ndarray
+    R: np.ndarray
+    t: np.ndarray
+
+    @property
+    def shape(self):
+        return self.gray_u8.shape
+
+
+def served_stream(seed: int = 0, duration_s: float = 60.0, rate_hz: float = 2.0, n_waypoints: int = 20,
+                  sizes=((1920, 960), (3840, 1920)), p_sizes=(0.75, 0.25), t_end: float | None = None,
+                  device: int = 0) -> list:
+    """Keyframes as a SLAM front end emits them: Poisson arrivals at rate_hz
+    along the hall scene's seeded smooth trajectory (duration_s seconds through
+    n_waypoints waypoints), each at a size drawn from `sizes` with
+    probabilities `p_sizes`.  Rendered on the GPU, returned on the host.
+    t_end stops the stream early (seconds)."""
+    import torch
+    rng = np.random.default_rng(seed)
+    sc = Scene(HALL, seed)
+    end = duration_s if t_end is None else min(t_end, duration_s)
+    times = []
+    t = rng.exponential(1.0 / rate_hz)
+    while t < end:
+        times.append(t)
+        t += rng.exponential(1.0 / rate_hz)
+    which = rng.choice(len(sizes), size=len(times), p=np.asarray(p_sizes, float) / np.sum(p_sizes))
+    out = []
+    dev = torch.device("cuda", device)
+    bufs = {}
+    for k, (ts, w) in enumerate(zip(times, which)):
+        W, H = sizes[w]
+        if (W, H) not in bufs:
+            bufs[(W, H)] = (torch.empty((H, W), dtype=torch.uint8, device=dev),
+                            torch.empty((H, W), dtype=torch.float32, device=dev))
+        g, d = bufs[(W, H)]
+        R, tc = sc.trajectory_pose(seed, n_waypoints, duration_s, ts)
+        sc.render_device(R, tc, W, H, gray=g, depth=d, stream=torch.cuda.current_stream(dev).cuda_stream)
+        out.append(Keyframe(float(ts), g.cpu().numpy(), d.cpu().numpy(), R, tc))
+    return out

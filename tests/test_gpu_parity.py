@@ -333,5 +333,16 @@ def test_prior_seeding_matches_oracle_and_speeds_convergence(ctx):
     (a_s, v_s), (a_u, v_u) = acc(s2), acc(u8)
     print(f"seeded-2 acc1% {a_s:.4f} valid {v_s:.3f} | unseeded-8 acc1% {a_u:.4f} valid {v_u:.3f}")
     assert a_s >= a_u - 0.02 and v_s >= v_u - 0.02
+    # a retained snapshot of A seeds exactly like A itself, after A is reused
+    res = native.Result(ctx, W, H)
+    res.snapshot(A)
+    A.set_views([imgs[3], imgs[2], imgs[1]], Rs[[3, 2, 1]], ts[[3, 2, 1]])
+    A.run()  # overwrites A's state; the snapshot is unaffected
+    B.set_params(native.default_params(iterations=2, keyframe_id=1))
+    B.set_prior(res)
+    B.run()
+    assert np.array_equal(B.read()["depth"], s2)
+    B.set_prior(None)
+    res.close()
     A.close()
     B.close()

@@ -1,0 +1,100 @@
+"""The served request loop (pm_server): continuous batching with results that
+do not depend on what else is in flight."""
+import numpy as np
+import pytest
+
+from patchmatch_gb300 import native, scene
+
+pytestmark = pytest.mark.gpu
+
+W, H = 384, 192
+
+
+@pytest.fixture(scope="module")
+def stream_views():
+    sc = scene.Scene(scene.ROOM_OBJECTS, 61)
+    views = []
+    for k in range(14):
+        R, t = sc.trajectory_pose(5, 8, 12.0, 0.5 + 0.3 * k)
+        views.append(sc.render(R, t, W, H))
+    return views
+
+
+def _cfg(inflight, **kw):
+    p = native.default_params(iterations=6)
+    return native.server_config(params=p, max_inflight=inflight, min_sources=2, max_sources=4, prior_lag=4,
+                                seeded_iterations=2, min_baseline=0.02, max_baseline=3.0, **kw)
+
+
+def _run(ctx, views, inflight, one_by_one):
+    srv = native.Server(ctx, _cfg(inflight))
+    out = {}
+    if one_by_one:
+        for k, v in enumerate(views):
+            tk = srv.submit(v.gray_u8, v.R, v.t)
+            out[k] = srv.wait(tk)
+    else:
+        tks = [srv.submit(v.gray_u8, v.R, v.t) for v in views]
+        for k, tk in enumerate(tks):
+            out[k] = srv.wait(tk)
+    srv.close()
+    return out
+
+
+def test_results_same_alone_and_in_the_mix(ctx, stream_views):
+    alone = _run(ctx, stream_views, 1, True)
+    mixed = _run(ctx, stream_views, 4, False)
+    n_dense = 0
+    for k in range(len(stream_views)):
+        ra, da, _, ia = alone[k]
+        rm, dm, _, im = mixed[k]
+        assert ra == rm, (k, ra, rm)
+        assert (ia["n_sources"], ia["seeded"], ia["iterations"]) == (im["n_sources"], im["seeded"], im["iterations"])
+        if ra == native.PM_OK:
+            n_dense += 1
+            assert np.array_equal(da, dm), k  # identical, not merely close
+    assert n_dense >= len(stream_views) - 3
+    # the first keyframes have too few earlier neighbours
+    assert alone[0][0] == native.PM_ENOTREADY
+    # later keyframes are seeded from an earlier result and sweep less
+    assert any(alone[k][3]["seeded"] for k in range(len(stream_views)))
+
+
+def test_seeded_served_quality(ctx, stream_views):
+    res = _run(ctx, stream_views, 4, False)
+    accs = []
+    for k, v in enumerate(stream_views):
+        rc, d, _, info = res[k]
+        if rc != native.PM_OK or not info["seeded"]:
+            continue
+        m = d > 0
+        accs.append((np.abs(d[m] - v.depth[m]) / v.depth[m] < 0.02).mean())
+    assert accs and np.mean(accs) > 0.5
+
+
+def test_admission_by_hbm_budget(built, stream_views):
+    one = native.lib().pm_request_bytes(W, H, 4, native.IMAGE_U8)
+    kept = native.lib().pm_result_bytes(W, H) * 6  # retained priors (at most prior_lag + 2 sizes in play)
+    c = native.Context(0, hbm_budget=int(one * 1.5) + kept)  # room for one request at a time
+    srv = native.Server(c, _cfg(4))
+    tks = [srv.submit(v.gray_u8, v.R, v.t) for v in stream_views[:8]]
+    res = [srv.wait(tk) for tk in tks]
+    srv.close()
+    c.close()
+    assert sum(r[0] == native.PM_OK for r in res) >= 5
+    assert all(r[0] in (native.PM_OK, native.PM_ENOTREADY) for r in res)
+
+
+def test_device_renderer_matches_host_renderer(built):
+    import torch
+    sc = scene.Scene(scene.ROOM_OBJECTS, 3)
+    R, t = sc.poses(1, 3, 0.2, 0.5, 15.0)
+    host = sc.render(R[0], t[0], 256, 128)
+    g = torch.zeros((128, 256), dtype=torch.uint8, device="cuda")
+    d = torch.zeros((128, 256), dtype=torch.float32, device="cuda")
+    sc.render_device(R[0], t[0], 256, 128, gray=g, depth=d)
+    torch.cuda.synchronize()
+    dd = d.cpu().numpy()
+    assert np.abs(dd - host.depth).max() / host.depth.max() < 1e-4
+    gg = g.cpu().numpy().astype(int)
+    assert np.mean(np.abs(gg - host.gray_u8.astype(int))) < 1.0
