@@ -69,6 +69,17 @@ extern "C" {
 #define PM_IMAGE_U8 0
 #define PM_IMAGE_F16 1
 
+/* Source-image sampling (pm_params.sampler).
+ *   PM_SAMPLER_EXACT  : bilinear interpolation with FP32 weights from
+ *                       quad-packed footprints (either seam policy).
+ *   PM_SAMPLER_TEXTURE: the GPU's texture filter, as the reference samples its
+ *                       source images (PatchMatchCuda.cu:146, 754-763): texel
+ *                       centres at +0.5, weights quantised to 1/256 of a
+ *                       texel, clamped at the image border (PM_SEAM_CLAMP
+ *                       only). */
+#define PM_SAMPLER_EXACT 0
+#define PM_SAMPLER_TEXTURE 1
+
 typedef struct {
     int patch_half;      /* taps at odd offsets -patch_half..patch_half (5 = PatchSize 7 - 2, depthmap.cc:725) */
     int iterations;      /* red-black sweeps (Dense.Iterations, config.cc:172) */
@@ -86,6 +97,7 @@ typedef struct {
     float sigma_x;
     uint32_t seed;       /* Philox key, with keyframe_id */
     uint32_t keyframe_id;
+    int sampler;         /* PM_SAMPLER_* */
 } pm_params;
 
 typedef struct {
@@ -110,7 +122,8 @@ typedef struct pm_result pm_result;
 
 /* Defaults of the reference path: patch_half 5, iterations 8, fold
  * combination, clamp seam, log-uniform/hemisphere init in [0.3, 20] m,
- * u8 images, post-processing on, min_score 0.1, sigmas 50/5. */
+ * u8 images, post-processing on, min_score 0.1, sigmas 50/5, texture
+ * sampler. */
 void pm_params_default(pm_params *p);
 
 /* Context: one CUDA stream on `device`, device buffers owned by the context,

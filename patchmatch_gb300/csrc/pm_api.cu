@@ -63,7 +63,10 @@ struct pm_request {
     void *block = nullptr;  // one device allocation holding everything below
     float *ref = nullptr;
     uint8_t *raw = nullptr;
-    void *quad[PM_MAX_SOURCES] = {};
+    void *quad[PM_MAX_SOURCES] = {};     // quad-packed footprints, or pitched images for textures
+    cudaTextureObject_t tex[PM_MAX_SOURCES] = {};
+    int tex_format = -1;                 // image format the texture objects were made for (-1: none)
+    size_t tex_pitch = 0;
     uint8_t *mask = nullptr;
     bool has_mask = false;
     float4 *plane = nullptr;
@@ -124,6 +127,10 @@ int fail(pm_ctx *ctx, int code, const char *fmt, ...) {
     } while (0)
 
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Start alignment of the per-source sampling buffers: texture objects bound
+// to pitched linear memory need the device's texture alignment (512 bytes).
+constexpr size_t kTexAlign = 512;
 
 int get_trig(pm_ctx *ctx, int W, int H, Trig *out) {
     for (const Trig &t : ctx->trig)
@@ -196,6 +203,9 @@ int validate_params(pm_ctx *ctx, const pm_params *p) {
         return fail(ctx, PM_EINVAL, "bad init_mode");
     if (p->image_format != PM_IMAGE_U8 && p->image_format != PM_IMAGE_F16)
         return fail(ctx, PM_EINVAL, "bad image_format");
+    if (p->sampler != PM_SAMPLER_EXACT && p->sampler != PM_SAMPLER_TEXTURE) return fail(ctx, PM_EINVAL, "bad sampler");
+    if (p->sampler == PM_SAMPLER_TEXTURE && p->seam != PM_SEAM_CLAMP)
+        return fail(ctx, PM_EINVAL, "the texture sampler clamps at the seam (needs PM_SEAM_CLAMP)");
     if (!(p->min_depth > 0.0f) || !(p->max_depth > p->min_depth) || !std::isfinite(p->max_depth))
         return fail(ctx, PM_EINVAL, "need 0 < min_depth < max_depth");
     if (!(p->sigma_color > 0.0f) || !(p->sigma_x > 0.0f)) return fail(ctx, PM_EINVAL, "sigmas must be > 0");
@@ -216,9 +226,10 @@ void fill_args(pm_request *r) {
     const pm_params &p = r->prm;
     for (int k = 0; k < r->S; ++k) {
         compose(r->R[0], r->t[0], r->R[k + 1], r->t[k + 1], a.P.M[k], a.P.c[k]);
-        a.quad[k] = r->quad[k];
+        a.src.quad[k] = r->quad[k];
+        a.src.tex[k] = (unsigned long long)r->tex[k];
     }
-    a.qpitch = r->W + 1;
+    a.src.qpitch = r->W + 1;
     a.row_trig = r->trig.row;
     a.col_trig = r->trig.col;
     a.ref = r->ref;
@@ -248,12 +259,67 @@ void fill_args(pm_request *r) {
     }
 }
 
+void destroy_textures(pm_request *r) {
+    for (int k = 0; k < r->S; ++k)
+        if (r->tex[k]) {
+            cudaDestroyTextureObject(r->tex[k]);
+            r->tex[k] = 0;
+        }
+    r->tex_format = -1;
+}
+
+// Texture objects over the sources' sampling buffers, which then hold the
+// images themselves at a texture-aligned pitch (the buffers are sized for
+// quads, (W+1)(H+1) x 4 or 8 bytes, which is always enough).  Bilinear
+// filter, clamp addressing, unnormalised coordinates; u8 texels read as
+// value / 255, half texels as values.
+int ensure_textures(pm_request *r) {
+    if (r->tex_format == r->prm.image_format) return PM_OK;
+    destroy_textures(r);
+    pm_ctx *ctx = r->ctx;
+    int align = 0, base_align = 0;
+    PM_CUDA(ctx, cudaDeviceGetAttribute(&align, cudaDevAttrTexturePitchAlignment, ctx->device));
+    PM_CUDA(ctx, cudaDeviceGetAttribute(&base_align, cudaDevAttrTextureAlignment, ctx->device));
+    for (int k = 0; k < r->S; ++k)
+        if (base_align > 0 && (uintptr_t)r->quad[k] % (uintptr_t)base_align)
+            return fail(ctx, PM_ECUDA, "sampling buffer not aligned to the texture alignment (%d bytes)", base_align);
+    const bool f16 = r->prm.image_format == PM_IMAGE_F16;
+    const size_t es = f16 ? 2 : 1;
+    const size_t a = (size_t)std::max(align, 32);
+    r->tex_pitch = ((size_t)r->W * es + a - 1) / a * a;
+    if (r->tex_pitch * r->H > (size_t)(r->W + 1) * (r->H + 1) * 4)
+        return fail(ctx, PM_EINVAL, "texture pitch %zu does not fit the sampling buffer", r->tex_pitch);
+    for (int k = 0; k < r->S; ++k) {
+        cudaResourceDesc res{};
+        res.resType = cudaResourceTypePitch2D;
+        res.res.pitch2D.devPtr = r->quad[k];
+        res.res.pitch2D.desc = f16 ? cudaCreateChannelDescHalf() : cudaCreateChannelDesc<uint8_t>();
+        res.res.pitch2D.width = r->W;
+        res.res.pitch2D.height = r->H;
+        res.res.pitch2D.pitchInBytes = r->tex_pitch;
+        cudaTextureDesc td{};
+        td.addressMode[0] = cudaAddressModeClamp;
+        td.addressMode[1] = cudaAddressModeClamp;
+        td.filterMode = cudaFilterModeLinear;
+        td.readMode = f16 ? cudaReadModeElementType : cudaReadModeNormalizedFloat;
+        td.normalizedCoords = 0;
+        if (cudaCreateTextureObject(&r->tex[k], &res, &td, nullptr) != cudaSuccess) {
+            cudaGetLastError();
+            destroy_textures(r);
+            return fail(ctx, PM_ECUDA, "texture object creation failed");
+        }
+    }
+    r->tex_format = r->prm.image_format;
+    return PM_OK;
+}
+
 int launch_tile(pm_request *r, int mode, int colour, int sweep) {
     pm::SweepArgs a = r->args;
     a.mode = mode;
     a.colour = colour;
     a.sweep = sweep;
-    cudaError_t e = pm::dispatch_tile(r->S, r->prm.image_format, pm::tile_grid(r->W, r->H), r->stream, a);
+    cudaError_t e = pm::dispatch_tile(r->S, pm::image_kind(r->prm.image_format, r->prm.sampler),
+                                      pm::tile_grid(r->W, r->H), r->stream, a);
     r->ctx->launches++;
     if (e != cudaSuccess) return fail(r->ctx, PM_ECUDA, "tile kernel launch: %s", cudaGetErrorString(e));
     return PM_OK;
@@ -370,34 +436,34 @@ int enqueue_run(pm_request *r) {
 namespace pm {
 dim3 tile_grid(int W, int H) { return dim3((W + kTileW - 1) / kTileW, (H + kTileH - 1) / kTileH); }
 
-cudaError_t dispatch_tile(int S, int fmt, dim3 grid, cudaStream_t st, const SweepArgs &a) {
+cudaError_t dispatch_tile(int S, int kind, dim3 grid, cudaStream_t st, const SweepArgs &a) {
     switch (S) {
-        case 1: return launch_tile<1>(fmt, grid, st, a);
-        case 2: return launch_tile<2>(fmt, grid, st, a);
-        case 3: return launch_tile<3>(fmt, grid, st, a);
-        case 4: return launch_tile<4>(fmt, grid, st, a);
-        case 5: return launch_tile<5>(fmt, grid, st, a);
-        case 6: return launch_tile<6>(fmt, grid, st, a);
-        case 7: return launch_tile<7>(fmt, grid, st, a);
-        case 8: return launch_tile<8>(fmt, grid, st, a);
-        case 9: return launch_tile<9>(fmt, grid, st, a);
-        case 10: return launch_tile<10>(fmt, grid, st, a);
+        case 1: return launch_tile<1>(kind, grid, st, a);
+        case 2: return launch_tile<2>(kind, grid, st, a);
+        case 3: return launch_tile<3>(kind, grid, st, a);
+        case 4: return launch_tile<4>(kind, grid, st, a);
+        case 5: return launch_tile<5>(kind, grid, st, a);
+        case 6: return launch_tile<6>(kind, grid, st, a);
+        case 7: return launch_tile<7>(kind, grid, st, a);
+        case 8: return launch_tile<8>(kind, grid, st, a);
+        case 9: return launch_tile<9>(kind, grid, st, a);
+        case 10: return launch_tile<10>(kind, grid, st, a);
         default: return cudaErrorInvalidValue;
     }
 }
 
-cudaError_t dispatch_hyp(int S, int fmt, int n, cudaStream_t st, const HypArgs &a) {
+cudaError_t dispatch_hyp(int S, int kind, int n, cudaStream_t st, const HypArgs &a) {
     switch (S) {
-        case 1: return launch_hyp<1>(fmt, n, st, a);
-        case 2: return launch_hyp<2>(fmt, n, st, a);
-        case 3: return launch_hyp<3>(fmt, n, st, a);
-        case 4: return launch_hyp<4>(fmt, n, st, a);
-        case 5: return launch_hyp<5>(fmt, n, st, a);
-        case 6: return launch_hyp<6>(fmt, n, st, a);
-        case 7: return launch_hyp<7>(fmt, n, st, a);
-        case 8: return launch_hyp<8>(fmt, n, st, a);
-        case 9: return launch_hyp<9>(fmt, n, st, a);
-        case 10: return launch_hyp<10>(fmt, n, st, a);
+        case 1: return launch_hyp<1>(kind, n, st, a);
+        case 2: return launch_hyp<2>(kind, n, st, a);
+        case 3: return launch_hyp<3>(kind, n, st, a);
+        case 4: return launch_hyp<4>(kind, n, st, a);
+        case 5: return launch_hyp<5>(kind, n, st, a);
+        case 6: return launch_hyp<6>(kind, n, st, a);
+        case 7: return launch_hyp<7>(kind, n, st, a);
+        case 8: return launch_hyp<8>(kind, n, st, a);
+        case 9: return launch_hyp<9>(kind, n, st, a);
+        case 10: return launch_hyp<10>(kind, n, st, a);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -425,6 +491,7 @@ void pm_params_default(pm_params *p) {
     p->sigma_x = 5.0f;
     p->seed = 0;
     p->keyframe_id = 0;
+    p->sampler = PM_SAMPLER_TEXTURE;
 }
 
 const char *pm_status_string(int s) {
@@ -538,7 +605,7 @@ size_t pm_request_bytes(int W, int H, int S, int fmt) {
     size_t b = 0;
     b += align256(N * 4);                 // ref
     b += align256(N * 2);                 // raw staging
-    b += (size_t)S * align256(NQ * qb);   // quads
+    b += (size_t)S * (align256(NQ * qb) + kTexAlign);  // quads (texture-aligned starts)
     b += align256(N);                     // mask
     b += align256(N * 16);                // plane
     b += align256(N * 4);                 // score
@@ -591,7 +658,11 @@ int pm_request_create(pm_ctx *ctx, int W, int H, int S, const pm_params *params,
     auto take = [&](size_t n) { void *q = p; p += align256(n); return q; };
     r->ref = (float *)take(N * 4);
     r->raw = (uint8_t *)take(N * 2);
-    for (int k = 0; k < S; ++k) r->quad[k] = take(NQ * qb);
+    for (int k = 0; k < S; ++k) {
+        // texture objects over these buffers need kTexAlign-aligned addresses
+        p = (char *)(((uintptr_t)p + kTexAlign - 1) / kTexAlign * kTexAlign);
+        r->quad[k] = take(NQ * qb);
+    }
     r->mask = (uint8_t *)take(N);
     r->plane = (float4 *)take(N * 16);
     r->score = (float *)take(N * 4);
@@ -620,6 +691,7 @@ int pm_request_destroy(pm_request *r) {
     cudaStreamSynchronize(r->stream);
     if (r->gexec) cudaGraphExecDestroy(r->gexec);
     if (r->graph) cudaGraphDestroy(r->graph);
+    destroy_textures(r);
     cudaEventDestroy(r->ready);
     cudaStreamDestroy(r->stream);
     cudaFree(r->block);
@@ -633,7 +705,8 @@ int pm_request_set_params(pm_request *r, const pm_params *params) {
     if (!r) return PM_EINVAL;
     int rc = validate_params(r->ctx, params);
     if (rc) return rc;
-    if (params->image_format != r->prm.image_format || params->seam != r->prm.seam) {
+    if (params->image_format != r->prm.image_format || params->seam != r->prm.seam ||
+        params->sampler != r->prm.sampler) {
         for (int k = 0; k <= r->S; ++k) r->have[k] = false;  // sampling images must be rebuilt
     }
     r->prm = *params;
@@ -652,6 +725,18 @@ int pm_request_set_view(pm_request *r, int k, const pm_view *v) {
     const size_t row = (size_t)r->W * es;
     const size_t pitch = v->pitch_bytes ? v->pitch_bytes : row;
     if (pitch < row) return fail(ctx, PM_EINVAL, "pitch %zu smaller than a row (%zu)", pitch, row);
+    if (k > 0 && r->prm.sampler == PM_SAMPLER_TEXTURE) {
+        // texture sampler: the source image itself, pitched for the texture unit
+        int rc = ensure_textures(r);
+        if (rc) return rc;
+        PM_CUDA(ctx, cudaMemcpy2DAsync(r->quad[k - 1], r->tex_pitch, v->gray, pitch, row, r->H, cudaMemcpyDefault,
+                                       r->stream));
+        std::memcpy(r->R[k], v->R_cw, sizeof(double) * 9);
+        std::memcpy(r->t[k], v->t_cw, sizeof(double) * 3);
+        r->have[k] = true;
+        r->graph_dirty = true;
+        return PM_OK;
+    }
     PM_CUDA(ctx, cudaMemcpy2DAsync(r->raw, row, v->gray, pitch, row, r->H, cudaMemcpyDefault, r->stream));
     if (k == 0) {
         pm::launch_ref_to_float(r->stream, r->raw, row, r->prm.image_format, r->W, r->H, r->ref);
@@ -979,8 +1064,11 @@ int pm_score_hypotheses(pm_request *r, int n, const int32_t *ij, const float *pl
     PM_CUDA(ctx, cudaMemcpyAsync(dpl, planes, (size_t)n * 12, cudaMemcpyHostToDevice, r->stream));
     pm::HypArgs a{};
     a.P = r->args.P;
-    for (int k = 0; k < r->S; ++k) a.quad[k] = r->quad[k];
-    a.qpitch = r->W + 1;
+    for (int k = 0; k < r->S; ++k) {
+        a.src.quad[k] = r->quad[k];
+        a.src.tex[k] = (unsigned long long)r->tex[k];
+    }
+    a.src.qpitch = r->W + 1;
     a.row_trig = r->trig.row;
     a.col_trig = r->trig.col;
     a.ref = r->ref;
@@ -1001,7 +1089,7 @@ int pm_score_hypotheses(pm_request *r, int n, const int32_t *ij, const float *pl
     a.scores = dsc;
     a.best = dbest;
     a.per_source = per_source ? dper : nullptr;
-    cudaError_t e = pm::dispatch_hyp(r->S, r->prm.image_format, n, r->stream, a);
+    cudaError_t e = pm::dispatch_hyp(r->S, pm::image_kind(r->prm.image_format, r->prm.sampler), n, r->stream, a);
     ctx->launches++;
     if (e != cudaSuccess) return fail(ctx, PM_ECUDA, "hypothesis kernel: %s", cudaGetErrorString(e));
     if (scores) PM_CUDA(ctx, cudaMemcpyAsync(scores, dsc, (size_t)n * 4, cudaMemcpyDeviceToHost, r->stream));

@@ -119,16 +119,18 @@ __device__ __forceinline__ void split_coord(float c, int &k, float &a) {
 }
 
 struct QuadU8 {
+    // sample coordinates: texel k at coordinate k
+    static constexpr float kCoordOffset = 0.0f;
     // shift: value subtracted from every texel, given as 2^23 + I_c so the
     // byte-to-float conversion and the centring are one subtraction.
     static __device__ __forceinline__ float shift_for(float centre) { return 8388608.0f + centre; }
-    static __device__ __forceinline__ float sample(const void *base, int pitch, float u, float v, float shift) {
+    static __device__ __forceinline__ float sample(const SrcSet &src, int r, float u, float v, float shift) {
         // u in [0, W], v in [0, H] by construction of the angle functions
         int x0, y0;
         float ax, ay;
         split_coord(u, x0, ax);
         split_coord(v, y0, ay);
-        const uint32_t w = __ldg(static_cast<const uint32_t *>(base) + (y0 * pitch + x0));
+        const uint32_t w = __ldg(static_cast<const uint32_t *>(src.quad[r]) + (y0 * src.qpitch + x0));
         // bytes -> floats minus the centre intensity: (2^23 + byte) - (2^23 + c)
         // texels as 2^23 + byte; differences are exact, the shift is applied once per row
         const float m00 = __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540));
@@ -142,19 +144,40 @@ struct QuadU8 {
 };
 
 struct QuadF16 {
+    static constexpr float kCoordOffset = 0.0f;
     static __device__ __forceinline__ float shift_for(float centre) { return centre; }
-    static __device__ __forceinline__ float sample(const void *base, int pitch, float u, float v, float shift) {
+    static __device__ __forceinline__ float sample(const SrcSet &src, int r, float u, float v, float shift) {
         int x0, y0;
         float ax, ay;
         split_coord(u, x0, ax);
         split_coord(v, y0, ay);
-        const uint2 w = __ldg(static_cast<const uint2 *>(base) + (y0 * pitch + x0));
+        const uint2 w = __ldg(static_cast<const uint2 *>(src.quad[r]) + (y0 * src.qpitch + x0));
         const float2 r0 = __half22float2(*reinterpret_cast<const __half2 *>(&w.x));
         const float2 r1 = __half22float2(*reinterpret_cast<const __half2 *>(&w.y));
         const float t00 = r0.x - shift, t01 = r0.y - shift, t10 = r1.x - shift, t11 = r1.y - shift;
         const float a = fmaf(ax, t01 - t00, t00);
         const float b = fmaf(ax, t11 - t10, t10);
         return fmaf(ay, b - a, a);
+    }
+};
+
+// Texture sampling (PM_SAMPLER_TEXTURE): the texture unit's bilinear filter
+// over the source image, read at the texel-centre convention of the
+// reference (coordinate + 0.5, PatchMatchCuda.cu:146), clamped at the border.
+// u8 images are bound as normalised 8-bit textures (value / 255).
+struct TexU8 {
+    static constexpr float kCoordOffset = 0.5f;
+    static __device__ __forceinline__ float shift_for(float centre) { return centre; }
+    static __device__ __forceinline__ float sample(const SrcSet &src, int r, float u, float v, float shift) {
+        return fmaf(tex2D<float>((cudaTextureObject_t)src.tex[r], u, v), 255.0f, -shift);
+    }
+};
+
+struct TexF16 {
+    static constexpr float kCoordOffset = 0.5f;
+    static __device__ __forceinline__ float shift_for(float centre) { return centre; }
+    static __device__ __forceinline__ float sample(const SrcSet &src, int r, float u, float v, float shift) {
+        return tex2D<float>((cudaTextureObject_t)src.tex[r], u, v) - shift;
     }
 };
 
@@ -203,11 +226,12 @@ struct TapAccum {
 #pragma unroll
         for (int r = 0; r < S; ++r) swy[r] = swyy[r] = swxy[r] = 0.0f;
     }
-    // P, quad, qpitch live in kernel parameter space; b: tap bearing,
-    // w: bilateral weight, xs: tap intensity minus centre.
-    __device__ __forceinline__ void add(const PmPoses &P, const void *const *quad, int qpitch, float Wf, float Hf,
-                                        float halfW, float halfH, float shift, float px, float py, float pz,
-                                        float bx, float by, float bz, float w, float xs) {
+    // P and src live in kernel parameter space; b: tap bearing,
+    // w: bilateral weight, xs: tap intensity minus centre; halfW/halfH
+    // include the sampler's coordinate offset.
+    __device__ __forceinline__ void add(const PmPoses &P, const SrcSet &src, float Wf, float Hf, float halfW,
+                                        float halfH, float shift, float px, float py, float pz, float bx, float by,
+                                        float bz, float w, float xs) {
         const float s = fmaf(px, bx, fmaf(py, by, pz * bz));
         const float as = fabsf(s);
         const uint32_t sg = __float_as_uint(s) & 0x80000000u;
@@ -227,7 +251,7 @@ struct TapAccum {
         }
 #pragma unroll
         for (int r = 0; r < S; ++r) {
-            const float y = Img::sample(quad[r], qpitch, u[r], v[r], shift);
+            const float y = Img::sample(src, r, u[r], v[r], shift);
             const float wy = w * y;
             swy[r] += wy;
             swyy[r] = fmaf(wy, y, swyy[r]);

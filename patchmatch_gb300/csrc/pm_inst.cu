@@ -17,32 +17,50 @@ cudaError_t tile_launch(dim3 grid, cudaStream_t st, const SweepArgs &a) {
 }
 }  // namespace
 
-// Opt both image variants in to > 48 KB of dynamic shared memory (called for
-// the current device when a context is created).
+namespace {
+template <class Img>
+cudaError_t tile_smem_attr() {
+    return cudaFuncSetAttribute(tile_kernel<PM_INST_S, Img>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)kTileSmemBytes);
+}
+template <class Img>
+cudaError_t hyp_launch(int n, cudaStream_t st, const HypArgs &a) {
+    hyp_kernel<PM_INST_S, Img><<<(n + 255) / 256, 256, 0, st>>>(a);
+    return cudaGetLastError();
+}
+}  // namespace
+
+// Set the dynamic shared memory limit of every image variant (called for the
+// current device when a context is created).
 template <int S>
 cudaError_t configure_tile();
 template <>
 cudaError_t configure_tile<PM_INST_S>() {
-    cudaError_t e = cudaFuncSetAttribute(tile_kernel<PM_INST_S, QuadU8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)kTileSmemBytes);
-    if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(tile_kernel<PM_INST_S, QuadF16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)kTileSmemBytes);
+    cudaError_t e = tile_smem_attr<QuadU8>();
+    e = e ? e : tile_smem_attr<QuadF16>();
+    e = e ? e : tile_smem_attr<TexU8>();
+    return e ? e : tile_smem_attr<TexF16>();
+}
+
+// kind: kImageQuadU8, kImageQuadF16, kImageTexU8, kImageTexF16
+template <>
+cudaError_t launch_tile<PM_INST_S>(int kind, dim3 grid, cudaStream_t st, const SweepArgs &a) {
+    switch (kind) {
+        case kImageQuadF16: return tile_launch<QuadF16>(grid, st, a);
+        case kImageTexU8: return tile_launch<TexU8>(grid, st, a);
+        case kImageTexF16: return tile_launch<TexF16>(grid, st, a);
+        default: return tile_launch<QuadU8>(grid, st, a);
+    }
 }
 
 template <>
-cudaError_t launch_tile<PM_INST_S>(int fmt, dim3 grid, cudaStream_t st, const SweepArgs &a) {
-    return fmt == PM_IMAGE_F16 ? tile_launch<QuadF16>(grid, st, a) : tile_launch<QuadU8>(grid, st, a);
-}
-
-template <>
-cudaError_t launch_hyp<PM_INST_S>(int fmt, int n, cudaStream_t st, const HypArgs &a) {
-    const int blocks = (n + 255) / 256;
-    if (fmt == PM_IMAGE_F16)
-        hyp_kernel<PM_INST_S, QuadF16><<<blocks, 256, 0, st>>>(a);
-    else
-        hyp_kernel<PM_INST_S, QuadU8><<<blocks, 256, 0, st>>>(a);
-    return cudaGetLastError();
+cudaError_t launch_hyp<PM_INST_S>(int kind, int n, cudaStream_t st, const HypArgs &a) {
+    switch (kind) {
+        case kImageQuadF16: return hyp_launch<QuadF16>(n, st, a);
+        case kImageTexU8: return hyp_launch<TexU8>(n, st, a);
+        case kImageTexF16: return hyp_launch<TexF16>(n, st, a);
+        default: return hyp_launch<QuadU8>(n, st, a);
+    }
 }
 
 }  // namespace pm

@@ -17,13 +17,20 @@ void launch_init_planes(cudaStream_t st, const float2 *row_trig, const float2 *c
 void launch_set_planes(cudaStream_t st, const float *planes3, const float *scores, const float2 *row_trig,
                        const float2 *col_trig, int W, int H, float4 *plane, float *score, int8_t *best);
 
+// Source-image variants of the tile and hypothesis kernels: image format x
+// sampler (quad-packed footprints or texture objects).
+enum { kImageQuadU8 = 0, kImageQuadF16 = 1, kImageTexU8 = 2, kImageTexF16 = 3 };
+inline int image_kind(int image_format, int sampler) {
+    return (sampler == PM_SAMPLER_TEXTURE ? 2 : 0) + (image_format == PM_IMAGE_F16 ? 1 : 0);
+}
+
 // pm_inst.cu (one translation unit per source count S)
 template <int S>
-cudaError_t launch_tile(int fmt, dim3 grid, cudaStream_t st, const SweepArgs &a);
+cudaError_t launch_tile(int kind, dim3 grid, cudaStream_t st, const SweepArgs &a);
 template <int S>
-cudaError_t launch_hyp(int fmt, int n, cudaStream_t st, const HypArgs &a);
-cudaError_t dispatch_tile(int S, int fmt, dim3 grid, cudaStream_t st, const SweepArgs &a);
-cudaError_t dispatch_hyp(int S, int fmt, int n, cudaStream_t st, const HypArgs &a);
+cudaError_t launch_hyp(int kind, int n, cudaStream_t st, const HypArgs &a);
+cudaError_t dispatch_tile(int S, int kind, dim3 grid, cudaStream_t st, const SweepArgs &a);
+cudaError_t dispatch_hyp(int S, int kind, int n, cudaStream_t st, const HypArgs &a);
 dim3 tile_grid(int W, int H);
 
 // pm_seed.cu: prior result -> seeding candidates of a new keyframe

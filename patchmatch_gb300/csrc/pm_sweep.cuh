@@ -51,6 +51,22 @@ constexpr size_t kTileSmemBytes = sizeof(float4) * kTileRows * kTileCols;
 template <int S>
 constexpr int tile_min_blocks() { return S <= 6 ? 3 : 2; }
 
+// Smoothness factor f in [0, 1] of a propagated plane p against the pixel's
+// current plane h and its depth before propagation (PatchMatchCuda.cu:322-337).
+__device__ __forceinline__ float smoothness_factor(float px, float py, float pz, float hx, float hy, float hz,
+                                                   float bxc, float byc, float bzc, float curr_depth) {
+    const float scale = __fadd_rn(__fadd_rn(__fmul_rn(px, bxc), __fmul_rn(py, byc)), __fmul_rn(pz, bzc));
+    const float denom = __fdiv_rn(1.0f, fmaxf(1e-6f, fabsf(scale)));
+    const float dq = __fdiv_rn(__fsub_rn(curr_depth, denom), curr_depth);
+    const float dsf = expf(__fmul_rn(-__fmul_rn(dq, dq), 1250.0f));
+    const float prod = __fadd_rn(__fadd_rn(__fmul_rn(hx, px), __fmul_rn(hy, py)), __fmul_rn(hz, pz));
+    const float ex = __fsub_rn(hx, px), ey = __fsub_rn(hy, py), ez = __fsub_rn(hz, pz);
+    const float nrm = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey)), __fmul_rn(ez, ez)));
+    const float ac = acosf(__fdiv_rn(prod, nrm));
+    const float psf = expf(__fmul_rn(-__fmul_rn(ac, ac), 8.0f));
+    return __fmul_rn(__fsub_rn(1.0f, dsf), __fsub_rn(1.0f, psf));
+}
+
 template <int S, class Img>
 __global__ void __launch_bounds__(kThreads, tile_min_blocks<S>()) tile_kernel(const __grid_constant__ SweepArgs a) {
     extern __shared__ float4 tile[];
@@ -103,43 +119,59 @@ __global__ void __launch_bounds__(kThreads, tile_min_blocks<S>()) tile_kernel(co
     float cx = hx, cy = hy, cz = hz, current_depth = curr_depth;
     float depth_hyp = 0.f;
     const float shift = Img::shift_for(Ic);
-    const float halfW = 0.5f * a.Wf, halfH = 0.5f * a.Hf;
+    const float halfW = fmaf(0.5f, a.Wf, Img::kCoordOffset), halfH = fmaf(0.5f, a.Hf, Img::kCoordOffset);
     const int nh = a.mode == kModeSweep ? 14 : 1;
 
+    // Propagated planes are scored as NCC x f with a smoothness factor
+    // f in [0, 1] that does not depend on the cost (PatchMatchCuda.cu:322-337).
+    // A candidate with 2 f <= score cannot be accepted by any combined score
+    // <= 2 (the exact NCC is bounded by 1), so its cost is not evaluated.
+    // Each lane walks its own pixel's hypotheses in order and passes over such
+    // candidates: a warp evaluates as many costs as its busiest lane needs.
+    int h = 0;
 #pragma unroll 1
-    for (int h = 0; h < nh; ++h) {
-        float px, py, pz;
-        if (a.mode == kModeScore) {
-            px = hx; py = hy; pz = hz;
-        } else if (a.mode == kModeSeed) {
-            px = cand.x; py = cand.y; pz = cand.z;
-        } else if (h < 8) {
-            // neighbours (0,1),(1,0),(0,-1),(-1,0),(0,3),(3,0),(0,-3),(-3,0) (PatchMatchCuda.cu:305)
-            const int sel = h & 3, far = (h >> 2) ? 3 : 1;
-            const int di = (sel == 1) ? far : (sel == 3 ? -far : 0);
-            const int dj = (sel == 0) ? far : (sel == 2 ? -far : 0);
-            const float4 np = a.plane[(size_t)(i + di) * W + (j + dj)];
-            px = np.x; py = np.y; pz = np.z;
-        } else {
-            const int t = h - 8;
-            if (t == 0) {
-                // current depth after propagation (PatchMatchCuda.cu:340-341)
-                const float dn = __fadd_rn(__fadd_rn(__fmul_rn(bxc, hx), __fmul_rn(byc, hy)), __fmul_rn(bzc, hz));
-                current_depth = __fdiv_rn(1.0f, fmaxf(1e-6f, fabsf(dn)));
-                cx = hx; cy = hy; cz = hz;
+    while (true) {
+        float px = 0.f, py = 0.f, pz = 0.f, f = 1.0f;
+        bool found = false;
+#pragma unroll 1
+        for (; h < nh; ++h) {
+            if (a.mode == kModeScore) {
+                px = hx; py = hy; pz = hz;
+            } else if (a.mode == kModeSeed) {
+                px = cand.x; py = cand.y; pz = cand.z;
+            } else if (h < 8) {
+                // neighbours (0,1),(1,0),(0,-1),(-1,0),(0,3),(3,0),(0,-3),(-3,0) (PatchMatchCuda.cu:305)
+                const int sel = h & 3, far = (h >> 2) ? 3 : 1;
+                const int di = (sel == 1) ? far : (sel == 3 ? -far : 0);
+                const int dj = (sel == 0) ? far : (sel == 2 ? -far : 0);
+                const float4 np = a.plane[(size_t)(i + di) * W + (j + dj)];
+                px = np.x; py = np.y; pz = np.z;
+                f = smoothness_factor(px, py, pz, hx, hy, hz, bxc, byc, bzc, curr_depth);
+                if (!(2.0f * f > score)) continue;  // cannot be accepted (also when f is NaN)
+            } else {
+                const int t = h - 8;
+                if (t == 0) {
+                    // current depth after propagation (PatchMatchCuda.cu:340-341)
+                    const float dn = __fadd_rn(__fadd_rn(__fmul_rn(bxc, hx), __fmul_rn(byc, hy)), __fmul_rn(bzc, hz));
+                    current_depth = __fdiv_rn(1.0f, fmaxf(1e-6f, fabsf(dn)));
+                    cx = hx; cy = hy; cz = hz;
+                }
+                // refinement t (PatchMatchCuda.cu:364-382) with Philox normals (tag sweep + 1)
+                float ra, rb, rc;
+                refine_normals(a.seed, a.keyframe, (uint32_t)idx, (uint32_t)(a.sweep + 1), t, ra, rb, rc);
+                depth_hyp = __fmul_rn(current_depth, expf(__fmul_rn(a.depth_range[t], ra)));
+                const float nr = a.normal_range[t];
+                const float nhx = __fadd_rn(cx, __fmul_rn(nr, ra));
+                const float nhy = __fadd_rn(cy, __fmul_rn(nr, rb));
+                const float nhz = __fadd_rn(cz, __fmul_rn(nr, rc));
+                const float qx = __fmul_rn(depth_hyp, bxc), qy = __fmul_rn(depth_hyp, byc), qz = __fmul_rn(depth_hyp, bzc);
+                const float den = __fadd_rn(__fadd_rn(__fmul_rn(nhx, qx), __fmul_rn(nhy, qy)), __fmul_rn(nhz, qz));
+                px = __fdiv_rn(nhx, den); py = __fdiv_rn(nhy, den); pz = __fdiv_rn(nhz, den);
             }
-            // refinement t (PatchMatchCuda.cu:364-382) with Philox normals (tag sweep + 1)
-            float ra, rb, rc;
-            refine_normals(a.seed, a.keyframe, (uint32_t)idx, (uint32_t)(a.sweep + 1), t, ra, rb, rc);
-            depth_hyp = __fmul_rn(current_depth, expf(__fmul_rn(a.depth_range[t], ra)));
-            const float nr = a.normal_range[t];
-            const float nhx = __fadd_rn(cx, __fmul_rn(nr, ra));
-            const float nhy = __fadd_rn(cy, __fmul_rn(nr, rb));
-            const float nhz = __fadd_rn(cz, __fmul_rn(nr, rc));
-            const float qx = __fmul_rn(depth_hyp, bxc), qy = __fmul_rn(depth_hyp, byc), qz = __fmul_rn(depth_hyp, bzc);
-            const float den = __fadd_rn(__fadd_rn(__fmul_rn(nhx, qx), __fmul_rn(nhy, qy)), __fmul_rn(nhz, qz));
-            px = __fdiv_rn(nhx, den); py = __fdiv_rn(nhy, den); pz = __fdiv_rn(nhz, den);
+            found = true;
+            break;
         }
+        if (!found) break;
 
         // ---- cost of hypothesis (px, py, pz) ----
         TapAccum<S, Img> acc;
@@ -155,7 +187,7 @@ __global__ void __launch_bounds__(kThreads, tile_min_blocks<S>()) tile_kernel(co
                 const int k2 = 2 * m2 - ph;
                 const float xs = e.w - Ic;
                 const float w = bilateral_weight(xs, a.ncf, fmaf((float)(k2 * k2), a.ndf, dk1));
-                acc.add(a.P, a.quad, a.qpitch, a.Wf, a.Hf, halfW, halfH, shift, px, py, pz, e.x, e.y, e.z, w, xs);
+                acc.add(a.P, a.src, a.Wf, a.Hf, halfW, halfH, shift, px, py, pz, e.x, e.y, e.z, w, xs);
             }
         }
         float sep[S], cum[S];
@@ -171,21 +203,12 @@ __global__ void __launch_bounds__(kThreads, tile_min_blocks<S>()) tile_kernel(co
                 cx = px; cy = py; cz = pz; score = sc; current_depth = cand.w; best = hb;
             }
         } else if (h < 8) {
-            // smoothness weighting of propagated planes (PatchMatchCuda.cu:322-337)
-            const float scale = __fadd_rn(__fadd_rn(__fmul_rn(px, bxc), __fmul_rn(py, byc)), __fmul_rn(pz, bzc));
-            const float denom = __fdiv_rn(1.0f, fmaxf(1e-6f, fabsf(scale)));
-            const float dq = __fdiv_rn(__fsub_rn(curr_depth, denom), curr_depth);
-            const float dsf = expf(__fmul_rn(-__fmul_rn(dq, dq), 1250.0f));
-            const float prod = __fadd_rn(__fadd_rn(__fmul_rn(hx, px), __fmul_rn(hy, py)), __fmul_rn(hz, pz));
-            const float ex = __fsub_rn(hx, px), ey = __fsub_rn(hy, py), ez = __fsub_rn(hz, pz);
-            const float nrm = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey)), __fmul_rn(ez, ez)));
-            const float ac = acosf(__fdiv_rn(prod, nrm));
-            const float psf = expf(__fmul_rn(-__fmul_rn(ac, ac), 8.0f));
-            sc = __fmul_rn(sc, __fmul_rn(__fsub_rn(1.0f, dsf), __fsub_rn(1.0f, psf)));
+            sc = __fmul_rn(sc, f);
             if (sc > score) { hx = px; hy = py; hz = pz; score = sc; best = hb; }
         } else {
             if (sc > score) { cx = px; cy = py; cz = pz; score = sc; current_depth = depth_hyp; best = hb; }
         }
+        ++h;
     }
 
     a.score[idx] = score;
@@ -210,7 +233,7 @@ __global__ void __launch_bounds__(256) hyp_kernel(const __grid_constant__ HypArg
     const float Ic = a.ref[(size_t)i * W + j];
     const float px = a.planes[3 * h], py = a.planes[3 * h + 1], pz = a.planes[3 * h + 2];
     const float shift = Img::shift_for(Ic);
-    const float halfW = 0.5f * a.Wf, halfH = 0.5f * a.Hf;
+    const float halfW = fmaf(0.5f, a.Wf, Img::kCoordOffset), halfH = fmaf(0.5f, a.Hf, Img::kCoordOffset);
     float sw = 0.f, swx = 0.f, swxx = 0.f;
     TapAccum<S, Img> acc;
     acc.zero();
@@ -226,7 +249,7 @@ __global__ void __launch_bounds__(256) hyp_kernel(const __grid_constant__ HypArg
             sw += w;
             swx = fmaf(w, xs, swx);
             swxx = fmaf(w * xs, xs, swxx);
-            acc.add(a.P, a.quad, a.qpitch, a.Wf, a.Hf, halfW, halfH, shift, px, py, pz, rt.x * ct.x, -rt.y,
+            acc.add(a.P, a.src, a.Wf, a.Hf, halfW, halfH, shift, px, py, pz, rt.x * ct.x, -rt.y,
                     rt.x * ct.y, w, xs);
         }
     }

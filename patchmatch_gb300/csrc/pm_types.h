@@ -16,11 +16,18 @@ struct PmPoses {
     float c[kMaxSrc][3];
 };
 
+// Per-source sampling images: quad-packed footprints (exact sampler) or
+// texture objects (texture sampler).
+struct SrcSet {
+    const void *quad[kMaxSrc];
+    unsigned long long tex[kMaxSrc];
+    int qpitch;  // quads per row (W + 1)
+};
+
 // Kernel arguments of the tile kernels (init scoring and red-black sweeps).
 struct SweepArgs {
     PmPoses P;
-    const void *quad[kMaxSrc];  // per-source quad-packed sampling images
-    int qpitch;                 // quads per row (W + 1)
+    SrcSet src;
     const float2 *row_trig;     // H entries: (cos lat, sin lat)
     const float2 *col_trig;     // W entries: (sin lon, cos lon)
     const float *ref;           // H x W reference intensities (float)
@@ -50,8 +57,7 @@ enum { kModeScore = 0, kModeSweep = 1, kModeSeed = 2 };
 // Arguments of the fixed-hypothesis scoring kernel.
 struct HypArgs {
     PmPoses P;
-    const void *quad[kMaxSrc];
-    int qpitch;
+    SrcSet src;
     const float2 *row_trig;
     const float2 *col_trig;
     const float *ref;

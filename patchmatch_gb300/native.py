@@ -17,6 +17,7 @@ COMBINE_FOLD, COMBINE_MAX, COMBINE_TOPK, COMBINE_FOLD_SEPARATE = 0, 1, 2, 3
 SEAM_CLAMP, SEAM_WRAP = 0, 1
 INIT_LOGUNIFORM_HEMI, INIT_REF_UNIFORM = 0, 1
 IMAGE_U8, IMAGE_F16 = 0, 1
+SAMPLER_EXACT, SAMPLER_TEXTURE = 0, 1
 MAX_SOURCES = 10
 
 # Every exported symbol declared in include/pm_gb300.h.
@@ -39,7 +40,7 @@ class Params(C.Structure):
                 ("seam", C.c_int), ("init_mode", C.c_int), ("image_format", C.c_int), ("postprocess", C.c_int),
                 ("min_depth", C.c_float), ("max_depth", C.c_float), ("min_score", C.c_float),
                 ("min_patch_sd", C.c_float), ("sigma_color", C.c_float), ("sigma_x", C.c_float),
-                ("seed", C.c_uint32), ("keyframe_id", C.c_uint32)]
+                ("seed", C.c_uint32), ("keyframe_id", C.c_uint32), ("sampler", C.c_int)]
 
 
 class View(C.Structure):

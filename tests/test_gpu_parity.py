@@ -33,6 +33,9 @@ def _hypotheses(req, n, seed, spread=0.25):
 
 
 def _req_on_gpu(ctx, req, **kw):
+    # exact FP32 bilinear weights unless a test asks for the texture sampler:
+    # the FP64 oracle then computes the same interpolation
+    kw.setdefault("sampler", native.SAMPLER_EXACT)
     p = native.default_params(**kw)
     r = ctx.request(req.W, req.H, req.n_src, p)
     if p.image_format == native.IMAGE_F16:
@@ -179,7 +182,7 @@ def test_densify_one_shot_equals_request_path(ctx, room):
     p = native.default_params(iterations=2)
     imgs = [v.gray_u8 for v in room.views]
     out = ctx.densify(imgs, room.R, room.t, p, want=("depth", "score"))
-    r = _req_on_gpu(ctx, room, iterations=2)
+    r = _req_on_gpu(ctx, room, iterations=2, sampler=native.SAMPLER_TEXTURE)
     r.run()
     b = r.read()
     assert np.array_equal(out["depth"], b["depth"])
@@ -290,12 +293,13 @@ def test_prior_seeding_matches_oracle_and_speeds_convergence(ctx):
     Rs = np.stack([v.R for v in views])
     ts = np.stack([v.t for v in views])
     # keyframe A = view 1 with sources 0, 2; keyframe B = view 2 with sources 1, 3
-    pa = native.default_params(iterations=8)
+    EX = native.SAMPLER_EXACT
+    pa = native.default_params(iterations=8, sampler=EX)
     A = ctx.request(W, H, 2, pa)
     A.set_views([imgs[1], imgs[0], imgs[2]], Rs[[1, 0, 2]], ts[[1, 0, 2]])
     A.run()
     a_out = A.read()
-    B = ctx.request(W, H, 2, native.default_params(iterations=0, postprocess=0, keyframe_id=1))
+    B = ctx.request(W, H, 2, native.default_params(iterations=0, postprocess=0, keyframe_id=1, sampler=EX))
     B.set_views([imgs[2], imgs[1], imgs[3]], Rs[[2, 1, 3]], ts[[2, 1, 3]])
     B.init()
     init = B.read(raw=True)
@@ -322,11 +326,11 @@ def test_prior_seeding_matches_oracle_and_speeds_convergence(ctx):
     def acc(d):
         v = d > 0
         return (np.abs(d[v] - gt[v]) / gt[v] < 0.01).mean(), v.mean()
-    B.set_params(native.default_params(iterations=2, keyframe_id=1))
+    B.set_params(native.default_params(iterations=2, keyframe_id=1, sampler=EX))
     B.set_prior(A)
     B.run()
     s2 = B.read()["depth"]
-    B.set_params(native.default_params(iterations=8, keyframe_id=1))
+    B.set_params(native.default_params(iterations=8, keyframe_id=1, sampler=EX))
     B.set_prior(None)
     B.run()
     u8 = B.read()["depth"]
@@ -338,7 +342,7 @@ def test_prior_seeding_matches_oracle_and_speeds_convergence(ctx):
     res.snapshot(A)
     A.set_views([imgs[3], imgs[2], imgs[1]], Rs[[3, 2, 1]], ts[[3, 2, 1]])
     A.run()  # overwrites A's state; the snapshot is unaffected
-    B.set_params(native.default_params(iterations=2, keyframe_id=1))
+    B.set_params(native.default_params(iterations=2, keyframe_id=1, sampler=EX))
     B.set_prior(res)
     B.run()
     assert np.array_equal(B.read()["depth"], s2)

@@ -36,6 +36,7 @@ def test_scene_library_exports(built):
 def test_params_default_and_status_strings(built):
     p = native.default_params()
     assert (p.patch_half, p.iterations, p.combine, p.seam) == (5, 8, native.COMBINE_FOLD, native.SEAM_CLAMP)
+    assert p.sampler == native.SAMPLER_TEXTURE
     assert abs(p.sigma_color - 50) < 1e-6 and abs(p.sigma_x - 5) < 1e-6 and abs(p.min_score - 0.1) < 1e-6
     L = native.lib()
     assert L.pm_status_string(native.PM_EBUDGET).decode() == "HBM budget exceeded"
