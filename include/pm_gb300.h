@@ -80,6 +80,17 @@ extern "C" {
 #define PM_SAMPLER_EXACT 0
 #define PM_SAMPLER_TEXTURE 1
 
+/* Propagation rule of the red-black sweeps (pm_params.propagation).
+ *   PM_PROPAGATION_SMOOTH: the reference GPU kernel (PatchMatchRedBlackPass_,
+ *     PatchMatchCuda.cu:273-407): neighbour planes scored x smoothness factor,
+ *     refinements around the plane after propagation.
+ *   PM_PROPAGATION_PLAIN: the reference's host variant (PatchMatchUpdatePixel,
+ *     depthmap.cc:1003-1067): plain score comparison, pixels and neighbours of
+ *     depth 0 ignored, each refinement around the current plane and depth with
+ *     its own depth draw, skipped (ranges kept) when the plane's z is 0. */
+#define PM_PROPAGATION_SMOOTH 0
+#define PM_PROPAGATION_PLAIN 1
+
 typedef struct {
     int patch_half;      /* taps at odd offsets -patch_half..patch_half (5 = PatchSize 7 - 2, depthmap.cc:725) */
     int iterations;      /* red-black sweeps (Dense.Iterations, config.cc:172) */
@@ -98,6 +109,7 @@ typedef struct {
     uint32_t seed;       /* Philox key, with keyframe_id */
     uint32_t keyframe_id;
     int sampler;         /* PM_SAMPLER_* */
+    int propagation;     /* PM_PROPAGATION_* */
 } pm_params;
 
 typedef struct {
@@ -123,7 +135,7 @@ typedef struct pm_result pm_result;
 /* Defaults of the reference path: patch_half 5, iterations 8, fold
  * combination, clamp seam, log-uniform/hemisphere init in [0.3, 20] m,
  * u8 images, post-processing on, min_score 0.1, sigmas 50/5, texture
- * sampler. */
+ * sampler, smooth (GPU) propagation. */
 void pm_params_default(pm_params *p);
 
 /* Context: one CUDA stream on `device`, device buffers owned by the context,
@@ -179,6 +191,19 @@ int pm_request_set_state(pm_request *req, const float *planes, const float *scor
  * alive and unchanged until the work is done.  Replaces the host
  * PreInitResultWarp (depthmap.cc:434-516); the prior's normals are rotated
  * into the new camera (the reference reuses them unrotated). */
+/* Seeding from SLAM landmarks (world points, n x 3 FP64): the GPU form of
+ * DepthmapEstimator::PreInitSparsePCL2 (depthmap.cc:361-432).  Each point is
+ * projected into the reference view in FP64 and rounded to the nearest pixel;
+ * the pixel's candidate plane faces the camera (normal = -bearing) at the
+ * point's range, and it replaces the current plane where it scores higher.
+ * Where several points land on one pixel the nearest is used (the reference
+ * resolves that by an OpenMP race).  pm_request_set_landmarks stages the
+ * points for pm_request_run (applied after the random initialisation and
+ * before the prior result, as in ComputePatchMatch, depthmap.cc:683-684);
+ * pm_request_seed_landmarks applies them to the current state now (and
+ * stages them too).  The reference view must be set first; n = 0 clears. */
+int pm_request_set_landmarks(pm_request *req, const double *xyz_world, int n);
+int pm_request_seed_landmarks(pm_request *req, const double *xyz_world, int n);
 int pm_request_seed(pm_request *req, const pm_request *prior);
 int pm_request_set_prior(pm_request *req, const pm_request *prior);
 /* Retained results: a compact copy (plane state + filtered depth + pose,

@@ -20,6 +20,7 @@ COMBINE_FOLD, COMBINE_MAX, COMBINE_TOPK, COMBINE_FOLD_SEPARATE = 0, 1, 2, 3
 SEAM_CLAMP, SEAM_WRAP = 0, 1
 ARITH_F64, ARITH_F32_REF = 0, 1
 INTERP_EXACT, INTERP_TEX8_RN, INTERP_TEX8_RZ = 0, 1, 2
+PROP_SMOOTH, PROP_PLAIN = 0, 1
 INIT_LOGUNIFORM_HEMI, INIT_REF_UNIFORM = 0, 1
 
 
@@ -51,7 +52,8 @@ class ORCostParams(C.Structure):
 class ORRunParams(C.Structure):
     _fields_ = [("cp", ORCostParams), ("iterations", C.c_int), ("min_depth", C.c_float),
                 ("max_depth", C.c_float), ("seed", C.c_uint32), ("keyframe", C.c_uint32),
-                ("init_mode", C.c_int), ("row_lo", C.c_int), ("row_hi", C.c_int), ("threads", C.c_int)]
+                ("init_mode", C.c_int), ("row_lo", C.c_int), ("row_hi", C.c_int), ("threads", C.c_int),
+                ("propagation", C.c_int)]
 
 
 _lib = None
@@ -137,9 +139,10 @@ def cost_batch(views: Views, cp: ORCostParams, ij, planes, threads: int = 0, wan
 
 
 def patchmatch(views: Views, cp: ORCostParams, iterations=8, min_depth=0.3, max_depth=20.0, seed=0,
-               keyframe=0, init_mode=INIT_LOGUNIFORM_HEMI, row_lo=-1, row_hi=-1, threads=0):
+               keyframe=0, init_mode=INIT_LOGUNIFORM_HEMI, row_lo=-1, row_hi=-1, threads=0, propagation=0):
     H, W = views.ref.shape
-    rp = ORRunParams(cp, iterations, min_depth, max_depth, seed, keyframe, init_mode, row_lo, row_hi, threads)
+    rp = ORRunParams(cp, iterations, min_depth, max_depth, seed, keyframe, init_mode, row_lo, row_hi, threads,
+                     propagation)
     plane = np.zeros((H, W, 3), np.float32)
     depth = np.zeros((H, W), np.float32)
     score = np.zeros((H, W), np.float32)
@@ -150,9 +153,9 @@ def patchmatch(views: Views, cp: ORCostParams, iterations=8, min_depth=0.3, max_
 
 
 def sweeps(views: Views, cp: ORCostParams, plane, depth, score, best, first_half, n_half, seed=0, keyframe=0,
-           row_lo=-1, row_hi=-1, threads=0):
+           row_lo=-1, row_hi=-1, threads=0, propagation=0):
     """Half-sweeps from a given state (arrays are copied, results returned)."""
-    rp = ORRunParams(cp, 0, 0.3, 20.0, seed, keyframe, INIT_LOGUNIFORM_HEMI, row_lo, row_hi, threads)
+    rp = ORRunParams(cp, 0, 0.3, 20.0, seed, keyframe, INIT_LOGUNIFORM_HEMI, row_lo, row_hi, threads, propagation)
     plane = np.ascontiguousarray(plane, np.float32).copy()
     depth = np.ascontiguousarray(depth, np.float32).copy()
     score = np.ascontiguousarray(score, np.float32).copy()
@@ -183,6 +186,50 @@ def warp_prior(prev_plane, prev_depth, Rp, tp, W, H, Rn, tn):
     cand = np.zeros((H, W, 4), np.float32)
     lib().or_warp_prior(Wp, Hp, _p(pl, _fp), _p(d, _fp), _p(Rp, _dp), _p(tp, _dp), W, H, _p(Rn, _dp), _p(tn, _dp),
                         _p(cand, _fp))
+    return cand
+
+
+def landmark_candidates(R, t, W, H, xyz, mask=None):
+    """Seeding candidates (H, W, 4) from SLAM landmarks: plane xyz + range
+    (0 = none).  Restates DepthmapEstimator::PreInitSparsePCL2
+    (depthmap.cc:361-432) in FP64: ReprojectEquirect (:143-161), nearest-pixel
+    rounding int(x + 0.5) (:380-381), mask test (:384-386), range = |X_c|
+    (:392), normal = -bearing and PlanePosFromDepthAndNormal_equirect
+    (:130-141, :395-400).  Where several landmarks land on one pixel the
+    nearest (then the lowest index) is kept; points rounding outside the image
+    are skipped."""
+    R = np.asarray(R, np.float64).reshape(3, 3)
+    t = np.asarray(t, np.float64).reshape(3)
+    cand = np.zeros((H, W, 4), np.float32)
+    best = {}
+    for k, p in enumerate(np.asarray(xyz, np.float64).reshape(-1, 3)):
+        X = R @ p + t
+        d = float(np.linalg.norm(X))
+        if d < 1e-4:
+            continue
+        b = X / d
+        lat = -np.arcsin(np.clip(b[1], -1.0, 1.0))
+        lon = np.arctan2(b[0], b[2])
+        x = W * (0.5 + lon / (2 * np.pi))
+        y = H * (0.5 - lat / np.pi)
+        x0, y0 = int(x + 0.5), int(y + 0.5)
+        if not (0 <= x0 < W and 0 <= y0 < H):
+            continue
+        key = (y0, x0)
+        df = float(np.float32(d))
+        if key not in best or (df, k) < best[key]:
+            best[key] = (df, k)
+    for (y0, x0), (df, k) in best.items():
+        if mask is not None and not mask[y0, x0]:
+            continue
+        bb = bearing64(W, H, y0, x0)
+        den = -df * float(np.dot(bb, bb))
+        if 0 <= den < 1e-5:
+            den = 1e-5
+        elif -1e-5 < den < 0:
+            den = -1e-5
+        cand[y0, x0, :3] = -bb / den
+        cand[y0, x0, 3] = df
     return cand
 
 

@@ -443,10 +443,82 @@ static void init_pixel(const or_views *v, const or_run_params *rp, int i, int j,
     *depth = d;
 }
 
+/* One pixel update of the reference's host variant (PatchMatchUpdatePixel,
+ * depthmap.cc:1003-1067; CheckPlaneCandidate :1069-1078): pixels and
+ * neighbours of depth 0 are ignored, candidates are compared by score alone
+ * and taken at once (plane, score, depth = DepthOfPlaneBackprojection :97-104);
+ * refinement t draws one depth normal and three normal-vector normals from
+ * Philox block t (tag sweep + 1), perturbs the current plane and depth, builds
+ * the plane with the 1e-5 clamp (:130-141) and is skipped without shrinking
+ * the ranges when the current plane's z is 0 (:1044-1046). */
+static void update_pixel_plain(const or_views *v, const or_run_params *rp, int sweep, int i, int j,
+                               float *plane, float *depthm, float *scorem, int32_t *bestm)
+{
+    const int W = v->W;
+    const size_t idx = (size_t)i * W + j;
+    static const int adjacent[8][2] = {{0, 1}, {1, 0}, {0, -1}, {-1, 0}, {0, 3}, {3, 0}, {0, -3}, {-3, 0}};
+    if (depthm[idx] == 0.0f) return;
+    float score = scorem[idx];
+    int best = bestm ? bestm[idx] : 0;
+    float cx = plane[3 * idx], cy = plane[3 * idx + 1], cz = plane[3 * idx + 2];
+    float cur_depth = depthm[idx];
+    float b[3];
+    run_bearing(v, &rp->cp, i, j, b);
+    for (int a = 0; a < 8; ++a) {
+        size_t n = (size_t)(i + adjacent[a][0]) * W + (j + adjacent[a][1]);
+        if (depthm[n] == 0.0f) continue;
+        float pl[3] = {plane[3 * n], plane[3 * n + 1], plane[3 * n + 2]};
+        int hb = 0;
+        float sc = run_cost(v, &rp->cp, i, j, pl, &hb);
+        if (sc > score) {
+            cx = pl[0]; cy = pl[1]; cz = pl[2]; score = sc; best = hb;
+            float dn = b[0] * cx + b[1] * cy + b[2] * cz;
+            cur_depth = 1 / fmaxf(1e-6f, fabsf(dn));
+        }
+    }
+    uint32_t w[24];
+    philox_words(rp->seed, rp->keyframe, (uint32_t)idx, (uint32_t)(sweep + 1), 6, w);
+    float depth_range = 0.02f, normal_range = 0.5f;
+    for (int t = 0; t < 6; ++t) {
+        if (cz == 0.0f) continue;
+        float z[4];
+        for (int q = 0; q < 2; ++q) {
+            float u1 = u24(w[4 * t + 2 * q]), u2 = u24(w[4 * t + 2 * q + 1]);
+            float r = sqrtf(-2.0f * logf(u1)), th = 6.28318530717958647692f * u2;
+            z[2 * q] = r * cosf(th);
+            z[2 * q + 1] = r * sinf(th);
+        }
+        float depth_hyp = cur_depth * expf(depth_range * z[0]);
+        float nhx = cx + normal_range * z[1], nhy = cy + normal_range * z[2], nhz = cz + normal_range * z[3];
+        float px = depth_hyp * b[0], py = depth_hyp * b[1], pz = depth_hyp * b[2];
+        float den = nhx * px + nhy * py + nhz * pz;
+        if (den < 1e-5f && den >= 0.0f) den = 1e-5f;
+        else if (den > -1e-5f && den < 0.0f) den = -1e-5f;
+        float pl[3] = {nhx / den, nhy / den, nhz / den};
+        int hb = 0;
+        float sc = run_cost(v, &rp->cp, i, j, pl, &hb);
+        if (sc > score) {
+            cx = pl[0]; cy = pl[1]; cz = pl[2]; score = sc; best = hb;
+            float dn = b[0] * cx + b[1] * cy + b[2] * cz;
+            cur_depth = 1 / fmaxf(1e-6f, fabsf(dn));
+        }
+        depth_range = (float)(depth_range * 0.3);
+        normal_range = (float)(normal_range * 0.8);
+    }
+    scorem[idx] = score;
+    plane[3 * idx] = cx; plane[3 * idx + 1] = cy; plane[3 * idx + 2] = cz;
+    depthm[idx] = cur_depth;
+    if (bestm) bestm[idx] = best;
+}
+
 /* One red/black pixel update (PatchMatchCuda.cu:287-404). */
 static void update_pixel(const or_views *v, const or_run_params *rp, int sweep, int i, int j,
                          float *plane, float *depthm, float *scorem, int32_t *bestm)
 {
+    if (rp->propagation == OR_PROP_PLAIN) {
+        update_pixel_plain(v, rp, sweep, i, j, plane, depthm, scorem, bestm);
+        return;
+    }
     const int W = v->W;
     const size_t idx = (size_t)i * W + j;
     static const int adjacent[8][2] = {{0, 1}, {1, 0}, {0, -1}, {-1, 0}, {0, 3}, {3, 0}, {0, -3}, {-3, 0}};

@@ -87,7 +87,13 @@ typedef struct {
     int init_mode;        /* OR_INIT_* */
     int row_lo, row_hi;   /* restrict updates to rows [row_lo, row_hi); -1,-1 = all */
     int threads;          /* OpenMP threads, 0 = default */
+    int propagation;      /* OR_PROP_* */
 } or_run_params;
+
+/* OR_PROP_SMOOTH: the reference GPU update (PatchMatchCuda.cu:287-404);
+ * OR_PROP_PLAIN: the reference host update (PatchMatchUpdatePixel,
+ * depthmap.cc:1003-1067) with Philox draws in place of mt19937. */
+enum { OR_PROP_SMOOTH = 0, OR_PROP_PLAIN = 1 };
 
 /* ---- random numbers ---- */
 void or_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);

@@ -79,6 +79,8 @@ struct pm_request {
     unsigned long long *zbuf = nullptr;  // splat depth test of the prior warp
     const pm_request *prior = nullptr;   // result reused as initialisation (may be null)
     const pm_result *prior_res = nullptr;
+    int2 *lm = nullptr;                  // landmark seeds (pixel index, depth bits), device
+    int n_lm = 0, lm_cap = 0;
     double R[PM_MAX_SOURCES + 1][9] = {}, t[PM_MAX_SOURCES + 1][3] = {};
     bool have[PM_MAX_SOURCES + 1] = {};
     Trig trig;
@@ -127,6 +129,12 @@ int fail(pm_ctx *ctx, int code, const char *fmt, ...) {
     } while (0)
 
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+int __float_as_int_host(float f) {
+    int i;
+    std::memcpy(&i, &f, sizeof i);
+    return i;
+}
 
 // Start alignment of the per-source sampling buffers: texture objects bound
 // to pitched linear memory need the device's texture alignment (512 bytes).
@@ -204,6 +212,8 @@ int validate_params(pm_ctx *ctx, const pm_params *p) {
     if (p->image_format != PM_IMAGE_U8 && p->image_format != PM_IMAGE_F16)
         return fail(ctx, PM_EINVAL, "bad image_format");
     if (p->sampler != PM_SAMPLER_EXACT && p->sampler != PM_SAMPLER_TEXTURE) return fail(ctx, PM_EINVAL, "bad sampler");
+    if (p->propagation != PM_PROPAGATION_SMOOTH && p->propagation != PM_PROPAGATION_PLAIN)
+        return fail(ctx, PM_EINVAL, "bad propagation");
     if (p->sampler == PM_SAMPLER_TEXTURE && p->seam != PM_SEAM_CLAMP)
         return fail(ctx, PM_EINVAL, "the texture sampler clamps at the seam (needs PM_SEAM_CLAMP)");
     if (!(p->min_depth > 0.0f) || !(p->max_depth > p->min_depth) || !std::isfinite(p->max_depth))
@@ -244,6 +254,7 @@ void fill_args(pm_request *r) {
     a.patch_half = p.patch_half;
     a.combine = p.combine;
     a.top_k = p.top_k;
+    a.propagation = p.propagation;
     a.seed = p.seed;
     a.keyframe = p.keyframe_id;
     a.color_factor = 1.0f / (2 * p.sigma_color * p.sigma_color);
@@ -422,8 +433,75 @@ int enqueue_seed_result(pm_request *r, const pm_result *res) {
     return enqueue_seed_from(r, PriorSrc{res->plane, res->fdepth, res->W, res->H, res->trig, res->R, res->t});
 }
 
+int enqueue_landmarks(pm_request *r) {
+    pm::launch_landmark_cands(r->stream, r->lm, r->n_lm, r->has_mask ? r->mask : nullptr, r->trig.row, r->trig.col,
+                              r->W, r->H, r->seed);
+    r->ctx->launches += r->n_lm > 0 ? 1 : 0;
+    for (int c = 0; c < 2; ++c) {
+        int rc = launch_tile(r, pm::kModeSeed, c, 0);
+        if (rc) return rc;
+    }
+    return PM_OK;
+}
+
+// Project world points into the reference view (FP64, ReprojectEquirect,
+// depthmap.cc:143-161), round to the nearest pixel (depthmap.cc:380-381) and
+// keep the nearest landmark per pixel (then the lowest index); upload the
+// list.  Points nearer than 1e-4 or rounding outside the image are skipped.
+int stage_landmarks(pm_request *r, const double *xyz, int n) {
+    pm_ctx *ctx = r->ctx;
+    if (n < 0 || (n > 0 && !xyz)) return fail(ctx, PM_EINVAL, "bad landmark array");
+    if (!r->have[0]) return fail(ctx, PM_EINVAL, "set the reference view before its landmarks");
+    const double *R = r->R[0], *t = r->t[0];
+    const double kPi = 3.14159265358979323846;
+    std::vector<std::pair<int, float>> best;  // (pixel, depth) after dedupe
+    std::vector<long long> key;               // per pixel in `best`: index into best
+    std::vector<std::pair<long long, std::pair<float, int>>> all;
+    all.reserve(n);
+    for (int k = 0; k < n; ++k) {
+        const double *p = xyz + 3 * (size_t)k;
+        if (!(std::isfinite(p[0]) && std::isfinite(p[1]) && std::isfinite(p[2])))
+            return fail(ctx, PM_EINVAL, "landmark %d is not finite", k);
+        const double X = R[0] * p[0] + R[1] * p[1] + R[2] * p[2] + t[0];
+        const double Y = R[3] * p[0] + R[4] * p[1] + R[5] * p[2] + t[1];
+        const double Z = R[6] * p[0] + R[7] * p[1] + R[8] * p[2] + t[2];
+        const double d = std::sqrt(X * X + Y * Y + Z * Z);
+        if (d < 1e-4) continue;
+        const double lat = -std::asin(std::max(-1.0, std::min(1.0, Y / d)));
+        const double lon = std::atan2(X, Z);
+        const double x = r->W * (0.5 + lon / (2.0 * kPi)), y = r->H * (0.5 - lat / kPi);
+        const int x0 = (int)(x + 0.5), y0 = (int)(y + 0.5);
+        if (x0 < 0 || y0 < 0 || x0 >= r->W || y0 >= r->H) continue;
+        all.push_back({(long long)y0 * r->W + x0, {(float)d, k}});
+    }
+    std::sort(all.begin(), all.end());  // by pixel, then depth, then landmark index
+    std::vector<int2> list;
+    for (size_t q = 0; q < all.size(); ++q)
+        if (q == 0 || all[q].first != all[q - 1].first)
+            list.push_back(make_int2((int)all[q].first, __float_as_int_host(all[q].second.first)));
+    if ((int)list.size() > r->lm_cap) {
+        if (r->lm) cudaFree(r->lm);
+        r->lm = nullptr;
+        r->lm_cap = 0;
+        if (cudaMalloc(&r->lm, list.size() * sizeof(int2)) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(ctx, PM_ENOMEM, "landmark buffer of %zu entries", list.size());
+        }
+        r->lm_cap = (int)list.size();
+        r->graph_dirty = true;
+    }
+    if (!list.empty())
+        PM_CUDA(ctx, cudaMemcpyAsync(r->lm, list.data(), list.size() * sizeof(int2), cudaMemcpyHostToDevice,
+                                     r->stream));
+    // the run graph is shaped by the count (one kernel more or less)
+    if ((int)list.size() != r->n_lm) r->graph_dirty = true;
+    r->n_lm = (int)list.size();
+    return PM_OK;
+}
+
 int enqueue_run(pm_request *r) {
     int rc = enqueue_init(r);
+    if (!rc && r->n_lm > 0) rc = enqueue_landmarks(r);
     if (!rc && r->prior) rc = enqueue_seed(r, r->prior);
     else if (!rc && r->prior_res) rc = enqueue_seed_result(r, r->prior_res);
     if (!rc) rc = enqueue_sweeps(r, 0, 2 * r->prm.iterations);
@@ -492,6 +570,7 @@ void pm_params_default(pm_params *p) {
     p->seed = 0;
     p->keyframe_id = 0;
     p->sampler = PM_SAMPLER_TEXTURE;
+    p->propagation = PM_PROPAGATION_SMOOTH;
 }
 
 const char *pm_status_string(int s) {
@@ -692,6 +771,7 @@ int pm_request_destroy(pm_request *r) {
     if (r->gexec) cudaGraphExecDestroy(r->gexec);
     if (r->graph) cudaGraphDestroy(r->graph);
     destroy_textures(r);
+    if (r->lm) cudaFree(r->lm);
     cudaEventDestroy(r->ready);
     cudaStreamDestroy(r->stream);
     cudaFree(r->block);
@@ -894,6 +974,24 @@ int pm_result_destroy(pm_result *res) {
     return PM_OK;
 }
 
+int pm_request_set_landmarks(pm_request *r, const double *xyz_world, int n) {
+    if (!r) return PM_EINVAL;
+    PM_CUDA(r->ctx, cudaSetDevice(r->ctx->device));
+    return stage_landmarks(r, xyz_world, n);
+}
+
+int pm_request_seed_landmarks(pm_request *r, const double *xyz_world, int n) {
+    if (!r) return PM_EINVAL;
+    int rc = check_views(r);
+    if (rc) return rc;
+    PM_CUDA(r->ctx, cudaSetDevice(r->ctx->device));
+    rc = stage_landmarks(r, xyz_world, n);
+    if (rc) return rc;
+    fill_args(r);
+    r->postprocessed = false;
+    return enqueue_landmarks(r);
+}
+
 int pm_request_seed(pm_request *r, const pm_request *prior) {
     if (!r || !prior) return fail(r ? r->ctx : nullptr, PM_EINVAL, "NULL argument");
     if (prior->ctx != r->ctx) return fail(r->ctx, PM_EINVAL, "prior belongs to another context");
@@ -954,7 +1052,7 @@ int pm_request_run(pm_request *r) {
     if (r->prior_res) PM_CUDA(ctx, cudaStreamWaitEvent(r->stream, r->prior_res->ready, 0));
     PM_CUDA(ctx, cudaGraphLaunch(r->gexec, r->stream));
     ctx->launches += 3 + 2 * (uint64_t)r->prm.iterations + (r->prm.postprocess ? 3 : 0) +
-                     ((r->prior || r->prior_res) ? 4 : 0);
+                     ((r->prior || r->prior_res) ? 4 : 0) + (r->n_lm > 0 ? 3 : 0);
     r->postprocessed = r->prm.postprocess != 0;
     return PM_OK;
 }

@@ -209,6 +209,19 @@ __device__ __forceinline__ void refine_normals(uint32_t seed, uint32_t kf, uint3
     rc = odd ? z[3] : z[2];
 }
 
+// The four standard normals of refinement t of the plain (host-variant)
+// propagation: Philox block t, words (x, y) and (z, w), one depth draw
+// followed by three normal draws (depthmap.cc:1041-1050).
+__device__ __forceinline__ void refine_normals4(uint32_t seed, uint32_t kf, uint32_t pix, uint32_t tag, int t,
+                                                float &z0, float &z1, float &z2, float &z3) {
+    const uint4 blk = philox_block(seed, kf, pix, tag, (uint32_t)t);
+    const float2 a = box_muller(blk.x, blk.y), b = box_muller(blk.z, blk.w);
+    z0 = a.x;
+    z1 = a.y;
+    z2 = b.x;
+    z3 = b.y;
+}
+
 // ---------------------------------------------------------------------------
 // One tap of the plane-induced warp for all S sources (PatchMatchCuda.cu:107-157,
 // restructured).  The reference maps X_c = b / (pi . b) through

@@ -12,7 +12,10 @@ namespace pm {
 namespace {
 template <class Img>
 cudaError_t tile_launch(dim3 grid, cudaStream_t st, const SweepArgs &a) {
-    tile_kernel<PM_INST_S, Img><<<grid, kThreads, kTileSmemBytes, st>>>(a);
+    if (a.propagation == PM_PROPAGATION_PLAIN)
+        tile_kernel<PM_INST_S, Img, true><<<grid, kThreads, kTileSmemBytes, st>>>(a);
+    else
+        tile_kernel<PM_INST_S, Img, false><<<grid, kThreads, kTileSmemBytes, st>>>(a);
     return cudaGetLastError();
 }
 }  // namespace
@@ -20,7 +23,10 @@ cudaError_t tile_launch(dim3 grid, cudaStream_t st, const SweepArgs &a) {
 namespace {
 template <class Img>
 cudaError_t tile_smem_attr() {
-    return cudaFuncSetAttribute(tile_kernel<PM_INST_S, Img>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(tile_kernel<PM_INST_S, Img, false>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmemBytes);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(tile_kernel<PM_INST_S, Img, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)kTileSmemBytes);
 }
 template <class Img>

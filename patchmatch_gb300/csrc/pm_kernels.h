@@ -47,6 +47,9 @@ struct WarpArgs {
     float4 *seed;                 // W*H candidates (w = range, 0 = none)
 };
 void launch_warp_prior(cudaStream_t st, const WarpArgs &a);
+// landmark seeds: lm[k] = (pixel index, depth bits), one per pixel
+void launch_landmark_cands(cudaStream_t st, const int2 *lm, int n, const uint8_t *mask, const float2 *row,
+                           const float2 *col, int W, int H, float4 *cand);
 
 // pm_post.cu
 struct PostArgs {

@@ -96,3 +96,40 @@ void launch_warp_prior(cudaStream_t st, const WarpArgs &a) {
 }
 
 }  // namespace pm
+
+// ---------------------------------------------------------------------------
+// Seeding from SLAM landmarks: the GPU half of the reference's
+// PreInitSparsePCL2 (depthmap.cc:361-432).  The host projects the landmarks
+// in FP64 and keeps the nearest landmark per pixel; here each one becomes the
+// candidate plane of its pixel with the normal facing the camera
+// (normal = -bearing, PlanePosFromDepthAndNormal_equirect, depthmap.cc:130-141).
+// ---------------------------------------------------------------------------
+namespace pm {
+namespace {
+
+__global__ void landmark_cand_kernel(const int2 *lm, int n, const uint8_t *mask, const float2 *row, const float2 *col,
+                                     int W, float4 *cand) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int idx = lm[k].x;
+    const float d = __int_as_float(lm[k].y);
+    if (mask && !mask[idx]) return;  // depthmap.cc:384-386
+    const int i = idx / W, j = idx - i * W;
+    const float2 rt = row[i], ct = col[j];
+    const float bx = rt.x * ct.x, by = -rt.y, bz = rt.x * ct.y;
+    // plane = n / (n . (d b)) with n = -b, |denominator| clamped to 1e-5
+    float den = -d * (bx * bx + by * by + bz * bz);
+    if (den < 1e-5f && den >= 0.0f) den = 1e-5f;
+    else if (den > -1e-5f && den < 0.0f) den = -1e-5f;
+    cand[idx] = make_float4(-bx / den, -by / den, -bz / den, d);
+}
+
+}  // namespace
+
+void launch_landmark_cands(cudaStream_t st, const int2 *lm, int n, const uint8_t *mask, const float2 *row,
+                           const float2 *col, int W, int H, float4 *cand) {
+    cudaMemsetAsync(cand, 0, (size_t)W * H * sizeof(float4), st);
+    if (n > 0) landmark_cand_kernel<<<(n + 255) / 256, 256, 0, st>>>(lm, n, mask, row, col, W, cand);
+}
+
+}  // namespace pm

@@ -67,7 +67,7 @@ __device__ __forceinline__ float smoothness_factor(float px, float py, float pz,
     return __fmul_rn(__fsub_rn(1.0f, dsf), __fsub_rn(1.0f, psf));
 }
 
-template <int S, class Img>
+template <int S, class Img, bool Plain>
 __global__ void __launch_bounds__(kThreads, tile_min_blocks<S>()) tile_kernel(const __grid_constant__ SweepArgs a) {
     extern __shared__ float4 tile[];
 
@@ -112,6 +112,8 @@ __global__ void __launch_bounds__(kThreads, tile_min_blocks<S>()) tile_kernel(co
         if (!(cand.w > 0.0f)) return;  // no candidate for this pixel
     }
     const float4 cur = a.plane[idx];
+    constexpr bool plain = Plain;  // PM_PROPAGATION_PLAIN (a separate instantiation)
+    if (a.mode == kModeSweep && plain && cur.w == 0.0f) return;  // ignored pixel (depthmap.cc:1007-1010)
     float score = a.score[idx];
     int best = a.best[idx];
     float hx = cur.x, hy = cur.y, hz = cur.z;   // plane_*_hyp of the reference
@@ -129,6 +131,8 @@ __global__ void __launch_bounds__(kThreads, tile_min_blocks<S>()) tile_kernel(co
     // Each lane walks its own pixel's hypotheses in order and passes over such
     // candidates: a warp evaluates as many costs as its busiest lane needs.
     int h = 0;
+    int kr = 0;            // plain propagation: refinements tried so far (their ranges shrink only when tried)
+    bool moved = false;    // plain propagation: a neighbour's plane was taken
 #pragma unroll 1
     while (true) {
         float px = 0.f, py = 0.f, pz = 0.f, f = 1.0f;
@@ -146,27 +150,53 @@ __global__ void __launch_bounds__(kThreads, tile_min_blocks<S>()) tile_kernel(co
                 const int dj = (sel == 0) ? far : (sel == 2 ? -far : 0);
                 const float4 np = a.plane[(size_t)(i + di) * W + (j + dj)];
                 px = np.x; py = np.y; pz = np.z;
-                f = smoothness_factor(px, py, pz, hx, hy, hz, bxc, byc, bzc, curr_depth);
-                if (!(2.0f * f > score)) continue;  // cannot be accepted (also when f is NaN)
+                if (plain) {
+                    if (np.w == 0.0f) continue;  // ignored neighbour (depthmap.cc:1018-1021)
+                } else {
+                    f = smoothness_factor(px, py, pz, hx, hy, hz, bxc, byc, bzc, curr_depth);
+                    if (!(2.0f * f > score)) continue;  // cannot be accepted (also when f is NaN)
+                }
             } else {
                 const int t = h - 8;
                 if (t == 0) {
-                    // current depth after propagation (PatchMatchCuda.cu:340-341)
+                    // current depth after propagation (PatchMatchCuda.cu:340-341); the
+                    // host variant keeps the stored depth unless a neighbour was taken
                     const float dn = __fadd_rn(__fadd_rn(__fmul_rn(bxc, hx), __fmul_rn(byc, hy)), __fmul_rn(bzc, hz));
-                    current_depth = __fdiv_rn(1.0f, fmaxf(1e-6f, fabsf(dn)));
+                    current_depth = (plain && !moved) ? curr_depth : __fdiv_rn(1.0f, fmaxf(1e-6f, fabsf(dn)));
                     cx = hx; cy = hy; cz = hz;
                 }
-                // refinement t (PatchMatchCuda.cu:364-382) with Philox normals (tag sweep + 1)
-                float ra, rb, rc;
-                refine_normals(a.seed, a.keyframe, (uint32_t)idx, (uint32_t)(a.sweep + 1), t, ra, rb, rc);
-                depth_hyp = __fmul_rn(current_depth, expf(__fmul_rn(a.depth_range[t], ra)));
-                const float nr = a.normal_range[t];
-                const float nhx = __fadd_rn(cx, __fmul_rn(nr, ra));
-                const float nhy = __fadd_rn(cy, __fmul_rn(nr, rb));
-                const float nhz = __fadd_rn(cz, __fmul_rn(nr, rc));
-                const float qx = __fmul_rn(depth_hyp, bxc), qy = __fmul_rn(depth_hyp, byc), qz = __fmul_rn(depth_hyp, bzc);
-                const float den = __fadd_rn(__fadd_rn(__fmul_rn(nhx, qx), __fmul_rn(nhy, qy)), __fmul_rn(nhz, qz));
-                px = __fdiv_rn(nhx, den); py = __fdiv_rn(nhy, den); pz = __fdiv_rn(nhz, den);
+                if (plain) {
+                    // refinement of the host variant (depthmap.cc:1035-1059): current
+                    // plane and depth, skipped without shrinking the ranges when
+                    // the plane's z is 0; plane from depth and normal with the
+                    // 1e-5 clamp (PlanePosFromDepthAndNormal_equirect, :130-141)
+                    if (cz == 0.0f) continue;
+                    float z0, z1, z2, z3;
+                    refine_normals4(a.seed, a.keyframe, (uint32_t)idx, (uint32_t)(a.sweep + 1), t, z0, z1, z2, z3);
+                    depth_hyp = __fmul_rn(current_depth, expf(__fmul_rn(a.depth_range[kr], z0)));
+                    const float nr = a.normal_range[kr];
+                    ++kr;
+                    const float nhx = __fadd_rn(cx, __fmul_rn(nr, z1));
+                    const float nhy = __fadd_rn(cy, __fmul_rn(nr, z2));
+                    const float nhz = __fadd_rn(cz, __fmul_rn(nr, z3));
+                    const float qx = __fmul_rn(depth_hyp, bxc), qy = __fmul_rn(depth_hyp, byc), qz = __fmul_rn(depth_hyp, bzc);
+                    float den = __fadd_rn(__fadd_rn(__fmul_rn(nhx, qx), __fmul_rn(nhy, qy)), __fmul_rn(nhz, qz));
+                    if (den < 1e-5f && den >= 0.0f) den = 1e-5f;
+                    else if (den > -1e-5f && den < 0.0f) den = -1e-5f;
+                    px = __fdiv_rn(nhx, den); py = __fdiv_rn(nhy, den); pz = __fdiv_rn(nhz, den);
+                } else {
+                    // refinement t (PatchMatchCuda.cu:364-382) with Philox normals (tag sweep + 1)
+                    float ra, rb, rc;
+                    refine_normals(a.seed, a.keyframe, (uint32_t)idx, (uint32_t)(a.sweep + 1), t, ra, rb, rc);
+                    depth_hyp = __fmul_rn(current_depth, expf(__fmul_rn(a.depth_range[t], ra)));
+                    const float nr = a.normal_range[t];
+                    const float nhx = __fadd_rn(cx, __fmul_rn(nr, ra));
+                    const float nhy = __fadd_rn(cy, __fmul_rn(nr, rb));
+                    const float nhz = __fadd_rn(cz, __fmul_rn(nr, rc));
+                    const float qx = __fmul_rn(depth_hyp, bxc), qy = __fmul_rn(depth_hyp, byc), qz = __fmul_rn(depth_hyp, bzc);
+                    const float den = __fadd_rn(__fadd_rn(__fmul_rn(nhx, qx), __fmul_rn(nhy, qy)), __fmul_rn(nhz, qz));
+                    px = __fdiv_rn(nhx, den); py = __fdiv_rn(nhy, den); pz = __fdiv_rn(nhz, den);
+                }
             }
             found = true;
             break;
@@ -204,9 +234,18 @@ __global__ void __launch_bounds__(kThreads, tile_min_blocks<S>()) tile_kernel(co
             }
         } else if (h < 8) {
             sc = __fmul_rn(sc, f);
-            if (sc > score) { hx = px; hy = py; hz = pz; score = sc; best = hb; }
+            if (sc > score) { hx = px; hy = py; hz = pz; score = sc; best = hb; moved = true; }
         } else {
-            if (sc > score) { cx = px; cy = py; cz = pz; score = sc; current_depth = depth_hyp; best = hb; }
+            if (sc > score) {
+                cx = px; cy = py; cz = pz; score = sc; best = hb;
+                if (plain) {
+                    // the host variant stores the plane's own depth (CheckPlaneCandidate, depthmap.cc:1074-1076)
+                    const float dn = __fadd_rn(__fadd_rn(__fmul_rn(bxc, px), __fmul_rn(byc, py)), __fmul_rn(bzc, pz));
+                    current_depth = __fdiv_rn(1.0f, fmaxf(1e-6f, fabsf(dn)));
+                } else {
+                    current_depth = depth_hyp;
+                }
+            }
         }
         ++h;
     }

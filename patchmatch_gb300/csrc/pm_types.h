@@ -42,6 +42,7 @@ struct SweepArgs {
     int sweep;                  // sweep index (Philox tag = sweep + 1)
     int mode;                   // 0 = score own plane, 1 = red-black update
     int combine, top_k;
+    int propagation;            // PM_PROPAGATION_*
     uint32_t seed, keyframe;
     float color_factor;         // 1 / (2 sigma_color^2)
     float dist_factor;          // 1 / (2 sigma_x^2)

@@ -18,6 +18,7 @@ SEAM_CLAMP, SEAM_WRAP = 0, 1
 INIT_LOGUNIFORM_HEMI, INIT_REF_UNIFORM = 0, 1
 IMAGE_U8, IMAGE_F16 = 0, 1
 SAMPLER_EXACT, SAMPLER_TEXTURE = 0, 1
+PROPAGATION_SMOOTH, PROPAGATION_PLAIN = 0, 1
 MAX_SOURCES = 10
 
 # Every exported symbol declared in include/pm_gb300.h.
@@ -26,7 +27,7 @@ EXPORTS = (
     "pm_stream", "pm_probe_fp32_peak",
     "pm_densify", "pm_request_create", "pm_request_destroy", "pm_request_bytes", "pm_request_set_params",
     "pm_request_set_view", "pm_request_init", "pm_request_set_state", "pm_request_sweep", "pm_request_postprocess",
-    "pm_request_seed", "pm_request_set_prior", "pm_result_bytes", "pm_result_create", "pm_result_snapshot",
+    "pm_request_seed", "pm_request_set_prior", "pm_request_set_landmarks", "pm_request_seed_landmarks", "pm_result_bytes", "pm_result_create", "pm_result_snapshot",
     "pm_result_destroy", "pm_request_set_prior_result",
     "pm_request_run", "pm_request_read", "pm_request_read_async", "pm_request_synchronize", "pm_request_query",
     "pm_request_stream", "pm_request_depth_device",
@@ -40,7 +41,7 @@ class Params(C.Structure):
                 ("seam", C.c_int), ("init_mode", C.c_int), ("image_format", C.c_int), ("postprocess", C.c_int),
                 ("min_depth", C.c_float), ("max_depth", C.c_float), ("min_score", C.c_float),
                 ("min_patch_sd", C.c_float), ("sigma_color", C.c_float), ("sigma_x", C.c_float),
-                ("seed", C.c_uint32), ("keyframe_id", C.c_uint32), ("sampler", C.c_int)]
+                ("seed", C.c_uint32), ("keyframe_id", C.c_uint32), ("sampler", C.c_int), ("propagation", C.c_int)]
 
 
 class View(C.Structure):
@@ -100,6 +101,8 @@ def lib():
     L.pm_request_set_state.argtypes = [_vp, _vp, _vp]
     L.pm_request_sweep.argtypes = [_vp, C.c_int, C.c_int]
     L.pm_request_seed.argtypes = [_vp, _vp]
+    L.pm_request_set_landmarks.argtypes = [_vp, _vp, C.c_int]
+    L.pm_request_seed_landmarks.argtypes = [_vp, _vp, C.c_int]
     L.pm_result_bytes.restype = _sz
     L.pm_result_bytes.argtypes = [C.c_int, C.c_int]
     L.pm_result_create.argtypes = [_vp, C.c_int, C.c_int, C.POINTER(_vp)]
@@ -343,6 +346,16 @@ class Request:
 
     def seed(self, prior: "Request"):
         self.ctx.check(self._L.pm_request_seed(self.h, prior.h))
+
+    def set_landmarks(self, xyz_world):
+        """Stage SLAM landmarks (n x 3 world points) for seeding in run()."""
+        xyz = np.ascontiguousarray(xyz_world, np.float64).reshape(-1, 3)
+        self.ctx.check(self._L.pm_request_set_landmarks(self.h, _ptr(xyz), xyz.shape[0]))
+
+    def seed_landmarks(self, xyz_world):
+        """Seed the current state from SLAM landmarks now."""
+        xyz = np.ascontiguousarray(xyz_world, np.float64).reshape(-1, 3)
+        self.ctx.check(self._L.pm_request_seed_landmarks(self.h, _ptr(xyz), xyz.shape[0]))
 
     def set_prior(self, prior: "Request | Result | None"):
         self._prior = prior  # keep it alive

@@ -124,3 +124,18 @@ def test_scene_ground_truth_consistent():
     assert np.isfinite(v.depth).all() and v.depth.min() > 0.1
     assert np.allclose(np.linalg.norm(v.normal, axis=2), 1.0, atol=1e-5)
     assert v.gray_u8.std() > 20
+
+
+def test_landmark_candidates_restatement():
+    """A landmark on the bearing of pixel (i, j) at range d gives that pixel
+    the camera-facing plane b / d; nearer landmarks win shared pixels; points
+    behind 1e-4 m or rounding outside the image give nothing."""
+    W, H = 64, 32
+    R = np.eye(3)
+    t = np.zeros(3)
+    b = O.bearing64(W, H, 10, 20)
+    pts = np.array([3.0 * b, 2.0 * b, [0.0, 0.0, 5e-5]])
+    c = O.landmark_candidates(R, t, W, H, pts)
+    assert c[10, 20, 3] == np.float32(2.0)
+    assert np.allclose(c[10, 20, :3], b / 2.0, rtol=1e-6)
+    assert (c[..., 3] > 0).sum() == 1
