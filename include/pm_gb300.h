@@ -347,6 +347,22 @@ int pm_fuse_noalloc(int width, int height, int n_views, float *const *depths, co
                     const double *t_cw, const uint8_t *bgr, float same_depth_threshold, float *pruned, float *xyz,
                     uint8_t *bgr_out, int32_t *ij, unsigned *count, void *stream);
 
+/* ---- neighbour geometry (host, FP64) ----
+ * pm_score_view: the densification thread's view test (score_view,
+ * depthmap_computation_module.cc:147-198; a keyframe joins the window when the
+ * score exceeds 0.25, :334-335): the fraction of landmarks common to both
+ * keyframes (matched by id) whose triangulation angle between the camera
+ * centres lies in (3, 30) degrees.  cur_xyz: n_cur x 3 world positions.
+ * No common landmark gives score 0.
+ * pm_depth_interval: the 10th / 90th percentile of the landmarks' ranges from
+ * the camera (keyframe::computePercentileDepth_10_90, data/keyframe.cc:428-455)
+ * and the densifier's depth interval [1e-5, 1.1 p90]
+ * (compute_depth_intervall, depthmap_computation_module.cc:123-131). */
+int pm_score_view(const double prev_center[3], const double cur_center[3], const uint64_t *prev_ids, int n_prev,
+                  const uint64_t *cur_ids, const double *cur_xyz, int n_cur, float *score, int *n_common);
+int pm_depth_interval(const double R_cw[9], const double t_cw[3], const double *xyz, int n, double *p10,
+                      double *p90, double *min_depth, double *max_depth);
+
 #ifdef __cplusplus
 }
 #endif

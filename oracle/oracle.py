@@ -301,3 +301,40 @@ def gt_plane(depth, normal, W, H, i, j):
     b = bearing64(W, H, i, j)
     n = np.asarray(normal, np.float64)
     return n / np.dot(n, depth * b)
+
+
+def score_view(prev_center, cur_center, prev_ids, cur_ids, cur_xyz):
+    """Neighbour view test (score_view, depthmap_computation_module.cc:147-198):
+    fraction of common landmarks (matched by id, first occurrence) whose angle
+    between the rays to the two camera centres lies in (pi/60, pi/6);
+    0 when there is none.  Returns (score, n_common)."""
+    prev = set(int(k) for k in prev_ids)
+    seen = set()
+    s, n = 0.0, 0
+    pc = np.asarray(prev_center, np.float64)
+    cc = np.asarray(cur_center, np.float64)
+    for k, lm in zip(cur_ids, np.asarray(cur_xyz, np.float64).reshape(-1, 3)):
+        k = int(k)
+        if k not in prev or k in seen:
+            continue
+        seen.add(k)
+        dp, dc = pc - lm, cc - lm
+        theta = np.arccos(np.dot(dc, dp) / np.sqrt(np.dot(dc, dc) * np.dot(dp, dp)))
+        if np.pi / 60 < theta < np.pi / 6:
+            s += 1.0
+        n += 1
+    return (np.float32(s) / np.float32(n) if n else 0.0), n
+
+
+def depth_interval(R_cw, t_cw, xyz):
+    """Landmark range percentiles (keyframe::computePercentileDepth_10_90,
+    data/keyframe.cc:428-455, ranges stored as float) and the densifier's
+    interval [1e-5, 1.1 p90] (compute_depth_intervall,
+    depthmap_computation_module.cc:123-131)."""
+    R = np.asarray(R_cw, np.float64).reshape(3, 3)
+    t = np.asarray(t_cw, np.float64).reshape(3)
+    X = np.asarray(xyz, np.float64).reshape(-1, 3) @ R.T + t
+    d = np.sort(np.linalg.norm(X, axis=1).astype(np.float32))
+    n = len(d)
+    p10, p90 = float(d[n // 10]), float(d[n // 10 * 9])
+    return p10, p90, 1e-5, p90 * 1.1

@@ -27,6 +27,7 @@ EXPORTS = (
     "pm_stream", "pm_probe_fp32_peak",
     "pm_densify", "pm_request_create", "pm_request_destroy", "pm_request_bytes", "pm_request_set_params",
     "pm_request_set_view", "pm_request_init", "pm_request_set_state", "pm_request_sweep", "pm_request_postprocess",
+    "pm_score_view", "pm_depth_interval",
     "pm_request_seed", "pm_request_set_prior", "pm_request_set_landmarks", "pm_request_seed_landmarks", "pm_result_bytes", "pm_result_create", "pm_result_snapshot",
     "pm_result_destroy", "pm_request_set_prior_result",
     "pm_request_run", "pm_request_read", "pm_request_read_async", "pm_request_synchronize", "pm_request_query",
@@ -126,6 +127,10 @@ def lib():
     L.pm_fuse.argtypes = [_vp, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, C.c_float, _vp, C.POINTER(Points)]
     L.pm_fuse_noalloc.argtypes = [C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, C.c_float, _vp, _vp, _vp, _vp, _vp,
                                   _vp]
+    L.pm_score_view.argtypes = [_vp, _vp, _vp, C.c_int, _vp, _vp, C.c_int, C.POINTER(C.c_float),
+                                C.POINTER(C.c_int)]
+    L.pm_depth_interval.argtypes = [_vp, _vp, _vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                    C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.pm_server_config_default.argtypes = [C.POINTER(ServerConfig)]
     L.pm_server_create.argtypes = [_vp, C.POINTER(ServerConfig), C.POINTER(_vp)]
     L.pm_server_submit.argtypes = [_vp, C.c_int, C.c_int, C.POINTER(View), C.POINTER(C.c_uint64)]
@@ -176,6 +181,35 @@ def make_view(gray, R, t, mask=None, pitch_bytes: int = 0) -> View:
     for a in range(3):
         v.t_cw[a] = t[a]
     return v
+
+
+def score_view(prev_center, cur_center, prev_ids, cur_ids, cur_xyz):
+    """pm_score_view: (score, n_common)."""
+    pc = np.ascontiguousarray(prev_center, np.float64)
+    cc = np.ascontiguousarray(cur_center, np.float64)
+    pi = np.ascontiguousarray(prev_ids, np.uint64)
+    ci = np.ascontiguousarray(cur_ids, np.uint64)
+    cx = np.ascontiguousarray(cur_xyz, np.float64).reshape(-1, 3)
+    if cx.shape[0] != len(ci):
+        raise ValueError("cur_ids and cur_xyz differ in length")
+    sc, nc = C.c_float(), C.c_int()
+    rc = lib().pm_score_view(_ptr(pc), _ptr(cc), _ptr(pi), len(pi), _ptr(ci), _ptr(cx), len(ci), C.byref(sc),
+                             C.byref(nc))
+    if rc != PM_OK:
+        raise PmError(rc, "pm_score_view failed")
+    return sc.value, nc.value
+
+
+def depth_interval(R_cw, t_cw, xyz):
+    """pm_depth_interval: (p10, p90, min_depth, max_depth)."""
+    R = np.ascontiguousarray(R_cw, np.float64)
+    t = np.ascontiguousarray(t_cw, np.float64)
+    x = np.ascontiguousarray(xyz, np.float64).reshape(-1, 3)
+    out = [C.c_double() for _ in range(4)]
+    rc = lib().pm_depth_interval(_ptr(R), _ptr(t), _ptr(x), x.shape[0], *[C.byref(o) for o in out])
+    if rc != PM_OK:
+        raise PmError(rc, "pm_depth_interval failed")
+    return tuple(o.value for o in out)
 
 
 class Context:
