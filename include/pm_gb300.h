@@ -347,6 +347,20 @@ int pm_fuse_noalloc(int width, int height, int n_views, float *const *depths, co
                     const double *t_cw, const uint8_t *bgr, float same_depth_threshold, float *pruned, float *xyz,
                     uint8_t *bgr_out, int32_t *ij, unsigned *count, void *stream);
 
+/* ---- dense map output (host) ----
+ * pm_write_ply: the fused points as ASCII PLY (x y z in fixed notation,
+ * colours as three uchar in stored order, white without colours), the file of
+ * map_database_io::save_point_cloud_dense (io/map_database_io.cc:45-80).
+ * pm_write_dense_msgpack: the dense map message of save_message_pack_dense
+ * (io/map_database_io.cc:22-43): a MessagePack map {cameras, keyframes,
+ * landmarks}, one landmark record per point in the layout of
+ * landmark::to_json (data/landmark.cc:370-377) with ids first_id, first_id+1,
+ * ... and keyframe_id as first and reference keyframe; the camera and
+ * keyframe tables (SLAM map state) are written empty.  Both return
+ * PM_EINVAL when the file cannot be written. */
+int pm_write_ply(const char *path, const pm_points *pts);
+int pm_write_dense_msgpack(const char *path, const pm_points *pts, uint64_t first_id, uint32_t keyframe_id);
+
 /* ---- neighbour geometry (host, FP64) ----
  * pm_score_view: the densification thread's view test (score_view,
  * depthmap_computation_module.cc:147-198; a keyframe joins the window when the

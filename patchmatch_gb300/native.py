@@ -27,7 +27,7 @@ EXPORTS = (
     "pm_stream", "pm_probe_fp32_peak",
     "pm_densify", "pm_request_create", "pm_request_destroy", "pm_request_bytes", "pm_request_set_params",
     "pm_request_set_view", "pm_request_init", "pm_request_set_state", "pm_request_sweep", "pm_request_postprocess",
-    "pm_score_view", "pm_depth_interval",
+    "pm_score_view", "pm_depth_interval", "pm_write_ply", "pm_write_dense_msgpack",
     "pm_request_seed", "pm_request_set_prior", "pm_request_set_landmarks", "pm_request_seed_landmarks", "pm_result_bytes", "pm_result_create", "pm_result_snapshot",
     "pm_result_destroy", "pm_request_set_prior_result",
     "pm_request_run", "pm_request_read", "pm_request_read_async", "pm_request_synchronize", "pm_request_query",
@@ -131,6 +131,8 @@ def lib():
                                 C.POINTER(C.c_int)]
     L.pm_depth_interval.argtypes = [_vp, _vp, _vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                     C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.pm_write_ply.argtypes = [C.c_char_p, C.POINTER(Points)]
+    L.pm_write_dense_msgpack.argtypes = [C.c_char_p, C.POINTER(Points), C.c_uint64, C.c_uint32]
     L.pm_server_config_default.argtypes = [C.POINTER(ServerConfig)]
     L.pm_server_create.argtypes = [_vp, C.POINTER(ServerConfig), C.POINTER(_vp)]
     L.pm_server_submit.argtypes = [_vp, C.c_int, C.c_int, C.POINTER(View), C.POINTER(C.c_uint64)]
@@ -198,6 +200,32 @@ def score_view(prev_center, cur_center, prev_ids, cur_ids, cur_xyz):
     if rc != PM_OK:
         raise PmError(rc, "pm_score_view failed")
     return sc.value, nc.value
+
+
+def _points(xyz, bgr):
+    xyz = np.ascontiguousarray(xyz, np.float64).reshape(-1, 3)
+    bgr = None if bgr is None else np.ascontiguousarray(bgr, np.uint8).reshape(-1, 3)
+    if bgr is not None and bgr.shape[0] != xyz.shape[0]:
+        raise ValueError("xyz and bgr differ in length")
+    n = xyz.shape[0]
+    return Points(n, n, xyz.ctypes.data if n else None, bgr.ctypes.data if (bgr is not None and n) else None,
+                  None), (xyz, bgr)
+
+
+def write_ply(path, xyz, bgr=None):
+    """pm_write_ply: ASCII PLY of points (n x 3 FP64) and colours (n x 3 u8)."""
+    pts, keep = _points(xyz, bgr)
+    rc = lib().pm_write_ply(str(path).encode(), C.byref(pts))
+    if rc != PM_OK:
+        raise PmError(rc, f"pm_write_ply failed for {path}")
+
+
+def write_dense_msgpack(path, xyz, bgr=None, first_id: int = 0, keyframe_id: int = 0):
+    """pm_write_dense_msgpack: the dense map message of the points."""
+    pts, keep = _points(xyz, bgr)
+    rc = lib().pm_write_dense_msgpack(str(path).encode(), C.byref(pts), first_id, keyframe_id)
+    if rc != PM_OK:
+        raise PmError(rc, f"pm_write_dense_msgpack failed for {path}")
 
 
 def depth_interval(R_cw, t_cw, xyz):
