@@ -347,6 +347,29 @@ int pm_fuse_noalloc(int width, int height, int n_views, float *const *depths, co
                     const double *t_cw, const uint8_t *bgr, float same_depth_threshold, float *pruned, float *xyz,
                     uint8_t *bgr_out, int32_t *ij, unsigned *count, void *stream);
 
+/* ---- input preparation (device buffers, context stream) ----
+ * The keyframe thumbnails the densifier reads (data/frame.cc:53-54,136-138)
+ * and the FP16 pyramid of the precision form.  All pointers are device
+ * memory; pitches in bytes; work is enqueued on the context's stream.
+ * pm_image_to_gray: 1, 3 or 4 interleaved channels in PM_ORDER_BGR or
+ *   PM_ORDER_RGB to gray with BT.601 weights in 14-bit fixed point, rounded
+ *   (the fixed-point form of the colour conversion in
+ *   util/image_converter.cc:8-39); 1 channel is copied.
+ * pm_image_resize: bilinear resize of 1-4 interleaved u8 channels, pixel
+ *   centres aligned, 11-bit fixed-point weights, one rounding (cv::resize's
+ *   linear scheme for thumbnails and masks).
+ * pm_build_pyramid_f16: out[0] = the u8 image as FP16 (W x H, tightly
+ *   packed), out[k] = 2x2 means of out[k-1] ((w+1)/2 x (h+1)/2, the last
+ *   row/column repeated at odd sizes), summed in FP32 and rounded once. */
+#define PM_ORDER_BGR 0
+#define PM_ORDER_RGB 1
+int pm_image_to_gray(pm_ctx *ctx, const void *src, int width, int height, size_t pitch, int channels, int order,
+                     void *gray, size_t gray_pitch);
+int pm_image_resize(pm_ctx *ctx, const void *src, int src_w, int src_h, size_t src_pitch, int channels, void *dst,
+                    int dst_w, int dst_h, size_t dst_pitch);
+int pm_build_pyramid_f16(pm_ctx *ctx, const void *src, int width, int height, size_t pitch, int levels,
+                         void *const *out);
+
 /* ---- dense map output (host) ----
  * pm_write_ply: the fused points as ASCII PLY (x y z in fixed notation,
  * colours as three uchar in stored order, white without colours), the file of

@@ -338,3 +338,57 @@ def depth_interval(R_cw, t_cw, xyz):
     n = len(d)
     p10, p90 = float(d[n // 10]), float(d[n // 10 * 9])
     return p10, p90, 1e-5, p90 * 1.1
+
+
+def to_gray(img, rgb=False):
+    """BT.601 gray in 14-bit fixed point, rounded (the fixed-point form of
+    COLOR_BGR2GRAY used by util/image_converter.cc:8-39)."""
+    img = np.asarray(img)
+    if img.ndim == 2:
+        return img.copy()
+    c = img.astype(np.uint32)
+    b, g, r = (c[..., 2], c[..., 1], c[..., 0]) if rgb else (c[..., 0], c[..., 1], c[..., 2])
+    return ((r * 4899 + g * 9617 + b * 1868 + 8192) >> 14).astype(np.uint8)
+
+
+def resize_linear(img, W, H):
+    """Bilinear resize, pixel centres aligned, 11-bit weights, one rounding
+    (the 8-bit linear resize scheme behind the thumbnails, data/frame.cc:53-54)."""
+    img = np.asarray(img)
+    h, w = img.shape[:2]
+    ch = 1 if img.ndim == 2 else img.shape[2]
+    src = img.reshape(h, w, ch).astype(np.int64)
+
+    def axis(n_dst, n_src):
+        f0 = (np.arange(n_dst, dtype=np.float32) + np.float32(0.5)) * np.float32(np.float32(n_src) / np.float32(n_dst)) \
+            - np.float32(0.5)
+        s = np.floor(f0).astype(np.int64)
+        f = (f0 - s.astype(np.float32)).astype(np.float32)
+        f[s < 0] = 0
+        s[s < 0] = 0
+        hi = s >= n_src - 1
+        f[hi] = 0
+        s[hi] = n_src - 1
+        c1 = np.rint(f * np.float32(2048)).astype(np.int64)
+        return s, np.minimum(s + 1, n_src - 1), 2048 - c1, c1
+
+    sx, sx1, cx0, cx1 = axis(W, w)
+    sy, sy1, cy0, cy1 = axis(H, h)
+    a = src[sy][:, sx] * cx0[None, :, None] + src[sy][:, sx1] * cx1[None, :, None]
+    b = src[sy1][:, sx] * cx0[None, :, None] + src[sy1][:, sx1] * cx1[None, :, None]
+    v = (a * cy0[:, None, None] + b * cy1[:, None, None] + (1 << 21)) >> 22
+    out = np.clip(v, 0, 255).astype(np.uint8)
+    return out[..., 0] if img.ndim == 2 else out
+
+
+def pyramid_f16(img, levels=3):
+    """FP16 pyramid: level 0 = the image, then 2x2 means (edge repeated)."""
+    out = [np.asarray(img).astype(np.float16)]
+    for _ in range(1, levels):
+        s = out[-1].astype(np.float32)
+        h, w = s.shape
+        ys = np.minimum(np.arange((h + 1) // 2) * 2 + np.array([[0], [1]]), h - 1)
+        xs = np.minimum(np.arange((w + 1) // 2) * 2 + np.array([[0], [1]]), w - 1)
+        t = s[ys[0]][:, xs[0]] + s[ys[0]][:, xs[1]] + s[ys[1]][:, xs[0]] + s[ys[1]][:, xs[1]]
+        out.append((np.float32(0.25) * t).astype(np.float16))
+    return out

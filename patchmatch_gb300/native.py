@@ -19,6 +19,7 @@ INIT_LOGUNIFORM_HEMI, INIT_REF_UNIFORM = 0, 1
 IMAGE_U8, IMAGE_F16 = 0, 1
 SAMPLER_EXACT, SAMPLER_TEXTURE = 0, 1
 PROPAGATION_SMOOTH, PROPAGATION_PLAIN = 0, 1
+ORDER_BGR, ORDER_RGB = 0, 1
 MAX_SOURCES = 10
 
 # Every exported symbol declared in include/pm_gb300.h.
@@ -28,6 +29,7 @@ EXPORTS = (
     "pm_densify", "pm_request_create", "pm_request_destroy", "pm_request_bytes", "pm_request_set_params",
     "pm_request_set_view", "pm_request_init", "pm_request_set_state", "pm_request_sweep", "pm_request_postprocess",
     "pm_score_view", "pm_depth_interval", "pm_write_ply", "pm_write_dense_msgpack",
+    "pm_image_to_gray", "pm_image_resize", "pm_build_pyramid_f16",
     "pm_request_seed", "pm_request_set_prior", "pm_request_set_landmarks", "pm_request_seed_landmarks", "pm_result_bytes", "pm_result_create", "pm_result_snapshot",
     "pm_result_destroy", "pm_request_set_prior_result",
     "pm_request_run", "pm_request_read", "pm_request_read_async", "pm_request_synchronize", "pm_request_query",
@@ -131,6 +133,9 @@ def lib():
                                 C.POINTER(C.c_int)]
     L.pm_depth_interval.argtypes = [_vp, _vp, _vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                     C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.pm_image_to_gray.argtypes = [_vp, _vp, C.c_int, C.c_int, _sz, C.c_int, C.c_int, _vp, _sz]
+    L.pm_image_resize.argtypes = [_vp, _vp, C.c_int, C.c_int, _sz, C.c_int, _vp, C.c_int, C.c_int, _sz]
+    L.pm_build_pyramid_f16.argtypes = [_vp, _vp, C.c_int, C.c_int, _sz, C.c_int, _vp]
     L.pm_write_ply.argtypes = [C.c_char_p, C.POINTER(Points)]
     L.pm_write_dense_msgpack.argtypes = [C.c_char_p, C.POINTER(Points), C.c_uint64, C.c_uint32]
     L.pm_server_config_default.argtypes = [C.POINTER(ServerConfig)]
@@ -280,6 +285,40 @@ class Context:
     def stream_handle(self) -> int:
         """cudaStream_t of the context (for torch.cuda.ExternalStream)."""
         return int(self._L.pm_stream(self.h))
+
+    # ---- input preparation (torch CUDA tensors in and out) ----
+    def to_gray(self, img, order: int = 0):
+        """(H, W, C) or (H, W) uint8 CUDA tensor -> (H, W) uint8 CUDA tensor."""
+        import torch
+        img = img.contiguous()
+        H, W = img.shape[:2]
+        ch = 1 if img.dim() == 2 else img.shape[2]
+        out = torch.empty((H, W), dtype=torch.uint8, device=img.device)
+        self.check(self._L.pm_image_to_gray(self.h, img.data_ptr(), W, H, W * ch, ch, order, out.data_ptr(), W))
+        return out
+
+    def resize(self, img, W: int, H: int):
+        """Bilinear resize of a (h, w[, C]) uint8 CUDA tensor to (H, W[, C])."""
+        import torch
+        img = img.contiguous()
+        h, w = img.shape[:2]
+        ch = 1 if img.dim() == 2 else img.shape[2]
+        out = torch.empty((H, W) + (() if img.dim() == 2 else (ch,)), dtype=torch.uint8, device=img.device)
+        self.check(self._L.pm_image_resize(self.h, img.data_ptr(), w, h, w * ch, ch, out.data_ptr(), W, H, W * ch))
+        return out
+
+    def pyramid_f16(self, img, levels: int = 3):
+        """FP16 pyramid of a (H, W) uint8 CUDA tensor: list of float16 tensors."""
+        import torch
+        img = img.contiguous()
+        H, W = img.shape
+        outs, w, h = [], W, H
+        for _ in range(levels):
+            outs.append(torch.empty((h, w), dtype=torch.float16, device=img.device))
+            w, h = (w + 1) // 2, (h + 1) // 2
+        arr = (C.c_void_p * levels)(*[o.data_ptr() for o in outs])
+        self.check(self._L.pm_build_pyramid_f16(self.h, img.data_ptr(), W, H, W, levels, arr))
+        return outs
 
     def probe_fp32_peak(self) -> float:
         v = C.c_double()
