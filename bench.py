@@ -276,6 +276,82 @@ def run_served(native, scene, ctx, local: int, args) -> dict:
     return out
 
 
+BATCH_SIZES = ((960, 480), (1920, 960), (2880, 1440), (3840, 1920))
+
+
+def run_batched(native, scene, ctx, local: int, args) -> dict:
+    """Batched form: requests of sizes drawn from BATCH_SIZES with 3-10
+    sources (room scenes, per-request seeds), densified one at a time
+    (pm_request_run) and as one batch (pm_batch, executor chosen by
+    pm_batch_tune on the first 16 requests)."""
+    import torch
+    rng = np.random.default_rng(12345)
+    reqs, work = [], 0.0
+    dev = torch.device("cuda", local)
+    for k in range(args.batched_requests):
+        W, H = BATCH_SIZES[rng.integers(len(BATCH_SIZES))]
+        S = int(rng.integers(3, 11))
+        sc = scene.Scene(scene.ROOM, 1000 + k)
+        R, t = sc.poses(S + 1, 1000 + k, 0.2, 0.5, 15.0)
+        r = ctx.request(W, H, S, native.default_params(iterations=SWEEPS, seed=k, keyframe_id=k))
+        img = torch.empty((H, W), dtype=torch.uint8, device=dev)
+        for v in range(S + 1):
+            sc.render_device(R[v], t[v], W, H, gray=img, stream=torch.cuda.current_stream(dev).cuda_stream)
+            torch.cuda.current_stream(dev).synchronize()
+            r.set_view(v, img.data_ptr(), R[v], t[v])
+            r.synchronize()
+        reqs.append(r)
+        work += W * H / 1e6 * S
+    torch.cuda.synchronize()
+    # plain: one keyframe at a time (each request's graph captured by an untimed run)
+    for r in reqs:
+        r.run()
+        r.synchronize()
+    t0 = time.perf_counter()
+    for r in reqs:
+        r.run()
+        r.synchronize()
+    plain_s = time.perf_counter() - t0
+    # batched: executor tuned on a subset, then the whole set in one graph
+    sub = native.Batch(ctx, reqs[:16])
+    tuning = sub.tune()
+    sub.close()
+    b = native.Batch(ctx, reqs)
+    b.set_executor(tuning["executor"], tuning["grid_mult"])
+    l0 = ctx.launches
+    b.run()
+    b.synchronize()
+    l1 = ctx.launches
+    stream = torch.cuda.ExternalStream(b.stream_handle)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        t1 = time.perf_counter()
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+        b.run()
+        with torch.cuda.stream(stream):
+            e1.record(stream)
+        b.synchronize()
+        batch_wall = time.perf_counter() - t1
+    batch_s = e0.elapsed_time(e1) / 1e3
+    b.close()
+    names = {native.BATCH_PERSISTENT: "persistent tile queue", native.BATCH_LAUNCHES: "per-request launches",
+             native.BATCH_STREAMS: "parallel graph branches"}
+    for r in reqs:
+        r.close()
+    return {"requests": len(reqs), "work_mpix_views": work,
+            "plain": {"value": work / plain_s, "seconds": plain_s, "form": "pm_request_run one at a time"},
+            "batched": {"value": work / batch_s, "seconds": batch_s, "wall_s": batch_wall,
+                        "executor": names[tuning["executor"]], "grid_mult": tuning["grid_mult"],
+                        "gpu_launches": int(l1 - l0), "clocks": clk.summary()},
+            "ratio_batched_over_plain": plain_s / batch_s,
+            "tuning_ms_first16": dict(zip(["persistent x1", "persistent x2", "per-request launches",
+                                           "parallel graph branches"], tuning["candidate_ms"])),
+            "workload": f"{len(reqs)} requests, sizes uniform over {[f'{w}x{h}' for w, h in BATCH_SIZES]}, 3-10 "
+                        f"sources, room scenes with per-request seeds, {SWEEPS} sweeps; results bit-identical "
+                        "between the forms"}
+
+
 def run_ours(args):
     import torch
     rank, ws, local, dist = _dist()
@@ -362,6 +438,7 @@ def run_ours(args):
     acc = float((np.abs(dn[m] - gt[m]) / gt[m] < 0.01).mean()) if m.any() else 0.0
 
     served = None if args.no_served else run_served(native, scene, ctx, local, args)
+    batched = None if args.no_batched else run_batched(native, scene, ctx, local, args)
     traffic = _traffic_from_profile()
     line = None
     if rank == 0:
@@ -389,6 +466,7 @@ def run_ours(args):
                          "flop_per_sample": FLOP_PER_SAMPLE, "samples_per_launch": _samples_per_half_sweep(),
                          "launch_ms": sweep_ms, "traffic": traffic},
             "served": served,
+            "batched": batched,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "gpu_launches": int(gpu_launches),
@@ -410,6 +488,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-served", action="store_true", help="skip the served-form measurement")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-form measurement")
+    ap.add_argument("--batched-requests", type=int, default=64, help="requests in the batched-form measurement")
     ap.add_argument("--served-rate", type=float, default=4.0, help="arrival rate of the capacity stream (Hz)")
     ap.add_argument("--served-seconds", type=float, default=30.0, help="length of the capacity stream (s)")
     ap.add_argument("--latency-seconds", type=float, default=20.0, help="length of the 10 Hz latency stream (s)")

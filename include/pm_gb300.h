@@ -131,6 +131,7 @@ typedef struct {
 typedef struct pm_ctx pm_ctx;
 typedef struct pm_request pm_request;
 typedef struct pm_result pm_result;
+typedef struct pm_batch pm_batch;
 
 /* Defaults of the reference path: patch_half 5, iterations 8, fold
  * combination, clamp seam, log-uniform/hemisphere init in [0.3, 20] m,
@@ -346,6 +347,42 @@ int pm_server_destroy(pm_server *srv);
 int pm_fuse_noalloc(int width, int height, int n_views, float *const *depths, const double *R_cw,
                     const double *t_cw, const uint8_t *bgr, float same_depth_threshold, float *pruned, float *xyz,
                     uint8_t *bgr_out, int32_t *ij, unsigned *count, void *stream);
+
+/* ---- batched form ----
+ * Many requests densified together: init scoring, every red/black half-sweep
+ * and the post-filter run phase-major over all requests, captured once into a
+ * CUDA graph and replayed by pm_batch_run.  Requests are grouped by source
+ * count, image variant, propagation rule and sweep count; each phase of a
+ * group is one persistent launch over a device queue of (request, 8x64 tile)
+ * items (PM_BATCH_PERSISTENT, grid = grid_mult x resident CTAs) or one launch
+ * per request (PM_BATCH_LAUNCHES); PM_BATCH_STREAMS instead runs each
+ * request's whole chain on one of 8 parallel graph branches (largest request
+ * first onto the least-loaded branch) so that requests overlap on the GPU.  Every request's maps equal those of
+ * pm_request_run bit for bit.  Requests keep their own buffers and streams:
+ * set their views before pm_batch_run; read them afterwards with
+ * pm_request_read (their streams wait for the batch).  Seeding (priors,
+ * landmarks) is not batched (PM_EINVAL).  pm_batch_tune runs the batch once
+ * per executor candidate, keeps the fastest and reports the timings.
+ * No counterpart in the reference (one keyframe at a time,
+ * depthmap_computation_module.cc:205-472). */
+#define PM_BATCH_PERSISTENT 0
+#define PM_BATCH_LAUNCHES 1
+#define PM_BATCH_STREAMS 2
+typedef struct {
+    int executor;            /* chosen PM_BATCH_* */
+    int grid_mult;           /* chosen persistent grid multiple */
+    float ms;                /* its time for one pm_batch_run */
+    float candidate_ms[4];   /* persistent x1, persistent x2, per-request launches, parallel branches */
+} pm_batch_tuning;
+int pm_batch_create(pm_ctx *ctx, pm_batch **out);
+int pm_batch_add(pm_batch *b, pm_request *req);
+int pm_batch_clear(pm_batch *b);
+int pm_batch_set_executor(pm_batch *b, int executor, int grid_mult);
+int pm_batch_run(pm_batch *b);
+int pm_batch_synchronize(pm_batch *b);
+void *pm_batch_stream(const pm_batch *b);
+int pm_batch_tune(pm_batch *b, pm_batch_tuning *out);
+int pm_batch_destroy(pm_batch *b);
 
 /* ---- input preparation (device buffers, context stream) ----
  * The keyframe thumbnails the densifier reads (data/frame.cc:53-54,136-138)

@@ -124,13 +124,14 @@ struct QuadU8 {
     // shift: value subtracted from every texel, given as 2^23 + I_c so the
     // byte-to-float conversion and the centring are one subtraction.
     static __device__ __forceinline__ float shift_for(float centre) { return 8388608.0f + centre; }
-    static __device__ __forceinline__ float sample(const SrcSet &src, int r, float u, float v, float shift) {
+    static __device__ __forceinline__ float sample(const void *quad, unsigned long long, int qpitch, float u, float v,
+                                                   float shift) {
         // u in [0, W], v in [0, H] by construction of the angle functions
         int x0, y0;
         float ax, ay;
         split_coord(u, x0, ax);
         split_coord(v, y0, ay);
-        const uint32_t w = __ldg(static_cast<const uint32_t *>(src.quad[r]) + (y0 * src.qpitch + x0));
+        const uint32_t w = __ldg(static_cast<const uint32_t *>(quad) + (y0 * qpitch + x0));
         // bytes -> floats minus the centre intensity: (2^23 + byte) - (2^23 + c)
         // texels as 2^23 + byte; differences are exact, the shift is applied once per row
         const float m00 = __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540));
@@ -146,12 +147,13 @@ struct QuadU8 {
 struct QuadF16 {
     static constexpr float kCoordOffset = 0.0f;
     static __device__ __forceinline__ float shift_for(float centre) { return centre; }
-    static __device__ __forceinline__ float sample(const SrcSet &src, int r, float u, float v, float shift) {
+    static __device__ __forceinline__ float sample(const void *quad, unsigned long long, int qpitch, float u, float v,
+                                                   float shift) {
         int x0, y0;
         float ax, ay;
         split_coord(u, x0, ax);
         split_coord(v, y0, ay);
-        const uint2 w = __ldg(static_cast<const uint2 *>(src.quad[r]) + (y0 * src.qpitch + x0));
+        const uint2 w = __ldg(static_cast<const uint2 *>(quad) + (y0 * qpitch + x0));
         const float2 r0 = __half22float2(*reinterpret_cast<const __half2 *>(&w.x));
         const float2 r1 = __half22float2(*reinterpret_cast<const __half2 *>(&w.y));
         const float t00 = r0.x - shift, t01 = r0.y - shift, t10 = r1.x - shift, t11 = r1.y - shift;
@@ -168,16 +170,18 @@ struct QuadF16 {
 struct TexU8 {
     static constexpr float kCoordOffset = 0.5f;
     static __device__ __forceinline__ float shift_for(float centre) { return centre; }
-    static __device__ __forceinline__ float sample(const SrcSet &src, int r, float u, float v, float shift) {
-        return fmaf(tex2D<float>((cudaTextureObject_t)src.tex[r], u, v), 255.0f, -shift);
+    static __device__ __forceinline__ float sample(const void *, unsigned long long tex, int, float u, float v,
+                                                   float shift) {
+        return fmaf(tex2D<float>((cudaTextureObject_t)tex, u, v), 255.0f, -shift);
     }
 };
 
 struct TexF16 {
     static constexpr float kCoordOffset = 0.5f;
     static __device__ __forceinline__ float shift_for(float centre) { return centre; }
-    static __device__ __forceinline__ float sample(const SrcSet &src, int r, float u, float v, float shift) {
-        return tex2D<float>((cudaTextureObject_t)src.tex[r], u, v) - shift;
+    static __device__ __forceinline__ float sample(const void *, unsigned long long tex, int, float u, float v,
+                                                   float shift) {
+        return tex2D<float>((cudaTextureObject_t)tex, u, v) - shift;
     }
 };
 
@@ -232,7 +236,45 @@ __device__ __forceinline__ void refine_normals4(uint32_t seed, uint32_t kf, uint
 // Moments are accumulated shifted by the centre intensity (y - I_c), which is
 // exact algebra for the NCC and avoids float cancellation in the variances.
 // ---------------------------------------------------------------------------
-template <int S, class Img>
+// Where the per-source constants of the sample loop come from.  ParamAccess:
+// kernel parameters (constant bank, usable directly as instruction operands).
+// SharedAccess: a request's arguments staged in shared memory by the batched
+// executor, re-read at every use: the loads are volatile so that the compiler
+// does not hoist all sources' rows into registers (that spills).
+struct ParamAccess {
+    static __device__ __forceinline__ float val(const float &x) { return x; }
+    static __device__ __forceinline__ float4 row(const float4 &g) { return g; }
+    static __device__ __forceinline__ unsigned long long tex(const unsigned long long &t) { return t; }
+    static __device__ __forceinline__ const void *ptr(const void *const &p) { return p; }
+};
+struct SharedAccess {
+    static __device__ __forceinline__ float val(const float &x) {
+        float v;
+        const unsigned a = (unsigned)__cvta_generic_to_shared(&x);
+        asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(a));
+        return v;
+    }
+    static __device__ __forceinline__ float4 row(const float4 &g) {
+        float4 v;
+        const unsigned a = (unsigned)__cvta_generic_to_shared(&g);
+        asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(a));
+        return v;
+    }
+    static __device__ __forceinline__ unsigned long long tex(const unsigned long long &t) {
+        unsigned long long v;
+        const unsigned a = (unsigned)__cvta_generic_to_shared(&t);
+        asm volatile("ld.shared.u64 %0, [%1];" : "=l"(v) : "r"(a));
+        return v;
+    }
+    static __device__ __forceinline__ const void *ptr(const void *const &p) {
+        unsigned long long v;
+        const unsigned a = (unsigned)__cvta_generic_to_shared(&p);
+        asm volatile("ld.shared.u64 %0, [%1];" : "=l"(v) : "r"(a));
+        return reinterpret_cast<const void *>(v);
+    }
+};
+
+template <int S, class Img, class Acc = ParamAccess>
 struct TapAccum {
     float swy[S], swyy[S], swxy[S];
     __device__ __forceinline__ void zero() {
@@ -256,15 +298,16 @@ struct TapAccum {
         float u[S], v[S];
 #pragma unroll
         for (int r = 0; r < S; ++r) {
-            const float X = fmaf(P.M[r][0], sbx, fmaf(P.M[r][1], sby, fmaf(P.M[r][2], sbz, as * P.c[r][0])));
-            const float Y = fmaf(P.M[r][3], sbx, fmaf(P.M[r][4], sby, fmaf(P.M[r][5], sbz, as * P.c[r][1])));
-            const float Z = fmaf(P.M[r][6], sbx, fmaf(P.M[r][7], sby, fmaf(P.M[r][8], sbz, as * P.c[r][2])));
+            const float4 g0 = Acc::row(P.G[r][0]), g1 = Acc::row(P.G[r][1]), g2 = Acc::row(P.G[r][2]);
+            const float X = fmaf(g0.x, sbx, fmaf(g0.y, sby, fmaf(g0.z, sbz, as * g0.w)));
+            const float Y = fmaf(g1.x, sbx, fmaf(g1.y, sby, fmaf(g1.z, sbz, as * g1.w)));
+            const float Z = fmaf(g2.x, sbx, fmaf(g2.y, sby, fmaf(g2.z, sbz, as * g2.w)));
             u[r] = fmaf(Wf, lon_turns(X, Z), halfW);
             v[r] = fmaf(Hf, lat_halfturns(X, Y, Z), halfH);
         }
 #pragma unroll
         for (int r = 0; r < S; ++r) {
-            const float y = Img::sample(src, r, u[r], v[r], shift);
+            const float y = Img::sample(Acc::ptr(src.quad[r]), Acc::tex(src.tex[r]), src.qpitch, u[r], v[r], shift);
             const float wy = w * y;
             swy[r] += wy;
             swyy[r] = fmaf(wy, y, swyy[r]);
@@ -342,8 +385,8 @@ __device__ __forceinline__ float combine_scores(const float (&sep)[S], const flo
 }
 
 // Per-source and cumulative NCCs of one hypothesis from the window moments.
-template <int S, class Img>
-__device__ __forceinline__ void source_nccs(const TapAccum<S, Img> &acc, float sw, float swx, float swxx, int mode,
+template <int S, class Img, class Acc>
+__device__ __forceinline__ void source_nccs(const TapAccum<S, Img, Acc> &acc, float sw, float swx, float swxx, int mode,
                                             float (&sep)[S], float (&cum)[S]) {
 #pragma unroll
     for (int r = 0; r < S; ++r) sep[r] = ncc_from_moments(sw, swx, swxx, acc.swy[r], acc.swyy[r], acc.swxy[r]);

@@ -18,9 +18,7 @@ cudaError_t tile_launch(dim3 grid, cudaStream_t st, const SweepArgs &a) {
         tile_kernel<PM_INST_S, Img, false><<<grid, kThreads, kTileSmemBytes, st>>>(a);
     return cudaGetLastError();
 }
-}  // namespace
 
-namespace {
 template <class Img>
 cudaError_t tile_smem_attr() {
     cudaError_t e = cudaFuncSetAttribute(tile_kernel<PM_INST_S, Img, false>,
@@ -34,7 +32,28 @@ cudaError_t hyp_launch(int n, cudaStream_t st, const HypArgs &a) {
     hyp_kernel<PM_INST_S, Img><<<(n + 255) / 256, 256, 0, st>>>(a);
     return cudaGetLastError();
 }
-}  // namespace
+
+template <class Img>
+cudaError_t batch_launch_img(bool plain, int blocks, cudaStream_t st, const BatchArgs &b) {
+    if (plain)
+        batch_kernel<PM_INST_S, Img, true><<<blocks, kThreads, kTileSmemBytes, st>>>(b);
+    else
+        batch_kernel<PM_INST_S, Img, false><<<blocks, kThreads, kTileSmemBytes, st>>>(b);
+    return cudaGetLastError();
+}
+
+template <class Img>
+int batch_occ(bool plain) {
+    int n = 0;
+    if (plain)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<PM_INST_S, Img, true>, kThreads, kTileSmemBytes);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<PM_INST_S, Img, false>, kThreads,
+                                                      kTileSmemBytes);
+    return n;
+}
+
+}  // namespace (helpers are per translation unit: each compiles one S)
 
 // Set the dynamic shared memory limit of every image variant (called for the
 // current device when a context is created).
@@ -56,6 +75,26 @@ cudaError_t launch_tile<PM_INST_S>(int kind, dim3 grid, cudaStream_t st, const S
         case kImageTexU8: return tile_launch<TexU8>(grid, st, a);
         case kImageTexF16: return tile_launch<TexF16>(grid, st, a);
         default: return tile_launch<QuadU8>(grid, st, a);
+    }
+}
+
+template <>
+cudaError_t launch_batch<PM_INST_S>(int kind, bool plain, int blocks, cudaStream_t st, const BatchArgs &b) {
+    switch (kind) {
+        case kImageQuadF16: return batch_launch_img<QuadF16>(plain, blocks, st, b);
+        case kImageTexU8: return batch_launch_img<TexU8>(plain, blocks, st, b);
+        case kImageTexF16: return batch_launch_img<TexF16>(plain, blocks, st, b);
+        default: return batch_launch_img<QuadU8>(plain, blocks, st, b);
+    }
+}
+
+template <>
+int batch_blocks_per_sm<PM_INST_S>(int kind, bool plain) {
+    switch (kind) {
+        case kImageQuadF16: return batch_occ<QuadF16>(plain);
+        case kImageTexU8: return batch_occ<TexU8>(plain);
+        case kImageTexF16: return batch_occ<TexF16>(plain);
+        default: return batch_occ<QuadU8>(plain);
     }
 }
 

@@ -29,7 +29,13 @@ template <int S>
 cudaError_t launch_tile(int kind, dim3 grid, cudaStream_t st, const SweepArgs &a);
 template <int S>
 cudaError_t launch_hyp(int kind, int n, cudaStream_t st, const HypArgs &a);
+template <int S>
+cudaError_t launch_batch(int kind, bool plain, int blocks, cudaStream_t st, const BatchArgs &b);
+template <int S>
+int batch_blocks_per_sm(int kind, bool plain);
 cudaError_t dispatch_tile(int S, int kind, dim3 grid, cudaStream_t st, const SweepArgs &a);
+cudaError_t dispatch_batch(int S, int kind, bool plain, int blocks, cudaStream_t st, const BatchArgs &b);
+int dispatch_batch_blocks_per_sm(int S, int kind, bool plain);
 cudaError_t dispatch_hyp(int S, int kind, int n, cudaStream_t st, const HypArgs &a);
 dim3 tile_grid(int W, int H);
 

@@ -67,12 +67,13 @@ __device__ __forceinline__ float smoothness_factor(float px, float py, float pz,
     return __fmul_rn(__fsub_rn(1.0f, dsf), __fsub_rn(1.0f, psf));
 }
 
-template <int S, class Img, bool Plain>
-__global__ void __launch_bounds__(kThreads, tile_min_blocks<S>()) tile_kernel(const __grid_constant__ SweepArgs a) {
-    extern __shared__ float4 tile[];
-
+// One tile visit: CTA-wide tile staging (one barrier), then per-thread work.
+// `a` is the kernel's parameter block (single-request launches) or a copy in
+// shared memory (the batched executor); (bx, by) is the tile index.
+template <int S, class Img, bool Plain, class Acc, class A>
+__device__ __forceinline__ void tile_body(const A &a, int bx, int by, float4 *tile) {
     const int tid = threadIdx.x, lane = tid & 31, ty = tid >> 5;
-    const int x0 = blockIdx.x * kTileW, i0 = blockIdx.y * kTileH;
+    const int x0 = bx * kTileW, i0 = by * kTileH;
     load_tile(tile, a.row_trig, a.col_trig, a.ref, a.W, a.H, i0, x0, a.colour);
     __syncthreads();
 
@@ -204,7 +205,7 @@ __global__ void __launch_bounds__(kThreads, tile_min_blocks<S>()) tile_kernel(co
         if (!found) break;
 
         // ---- cost of hypothesis (px, py, pz) ----
-        TapAccum<S, Img> acc;
+        TapAccum<S, Img, Acc> acc;
         acc.zero();
 #pragma unroll 1
         for (int m1 = 0; m1 < nt; ++m1) {
@@ -216,12 +217,13 @@ __global__ void __launch_bounds__(kThreads, tile_min_blocks<S>()) tile_kernel(co
                 const float4 e = trow[m2];
                 const int k2 = 2 * m2 - ph;
                 const float xs = e.w - Ic;
-                const float w = bilateral_weight(xs, a.ncf, fmaf((float)(k2 * k2), a.ndf, dk1));
-                acc.add(a.P, a.src, a.Wf, a.Hf, halfW, halfH, shift, px, py, pz, e.x, e.y, e.z, w, xs);
+                const float w = bilateral_weight(xs, Acc::val(a.ncf), fmaf((float)(k2 * k2), Acc::val(a.ndf), dk1));
+                acc.add(a.P, a.src, Acc::val(a.Wf), Acc::val(a.Hf), halfW, halfH, shift, px, py, pz, e.x, e.y, e.z, w,
+                        xs);
             }
         }
         float sep[S], cum[S];
-        source_nccs<S, Img>(acc, sw, swx, swxx, a.combine, sep, cum);
+        source_nccs(acc, sw, swx, swxx, a.combine, sep, cum);
         int hb;
         float sc = combine_scores<S>(sep, cum, a.combine, a.top_k, &hb);
 
@@ -260,6 +262,45 @@ __global__ void __launch_bounds__(kThreads, tile_min_blocks<S>()) tile_kernel(co
     }
 }
 
+template <int S, class Img, bool Plain>
+__global__ void __launch_bounds__(kThreads, tile_min_blocks<S>()) tile_kernel(const __grid_constant__ SweepArgs a) {
+    extern __shared__ float4 tile[];
+    tile_body<S, Img, Plain, ParamAccess>(a, blockIdx.x, blockIdx.y, tile);
+}
+
+// Batched executor: a persistent grid walks a device queue of (request,
+// tile) work items of one phase (init scoring or one red/black half-sweep)
+// over many requests with the same source count and image variant.  Each CTA
+// takes the next item with one atomic, copies that request's arguments into
+// shared memory and visits the tile.  Items of one phase never depend on each
+// other (a half-sweep reads only the other colour), so no CTA waits on
+// another; phases are separated by kernel boundaries.
+template <int S, class Img, bool Plain>
+__global__ void __launch_bounds__(kThreads, tile_min_blocks<S>()) batch_kernel(const __grid_constant__ BatchArgs b) {
+    extern __shared__ float4 tile[];
+    __shared__ SweepArgs sa;
+    __shared__ int s_item;
+    for (;;) {
+        if (threadIdx.x == 0) s_item = (int)atomicAdd(b.counter, 1u);
+        __syncthreads();
+        const int it = s_item;
+        if (it >= b.n_items) return;
+        const int4 w = b.items[it];
+        const int4 *src = reinterpret_cast<const int4 *>(b.args + w.x);
+        int4 *dst = reinterpret_cast<int4 *>(&sa);
+        for (int k = threadIdx.x; k < (int)(sizeof(SweepArgs) / 16); k += blockDim.x) dst[k] = src[k];
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            sa.mode = b.mode;
+            sa.colour = b.colour;
+            sa.sweep = b.sweep;
+        }
+        __syncthreads();
+        tile_body<S, Img, Plain, SharedAccess>(sa, w.y, w.z, tile);
+        __syncthreads();  // before the next item replaces the arguments and the tile
+    }
+}
+
 // Fixed-hypothesis scoring: one thread per (pixel, plane); taps read straight
 // from global memory (L1-resident) instead of a staged tile.  Same per-tap
 // arithmetic (TapAccum) as the tile kernel.
@@ -293,7 +334,7 @@ __global__ void __launch_bounds__(256) hyp_kernel(const __grid_constant__ HypArg
         }
     }
     float sep[S], cum[S];
-    source_nccs<S, Img>(acc, sw, swx, swxx, a.combine, sep, cum);
+    source_nccs(acc, sw, swx, swxx, a.combine, sep, cum);
     if (a.per_source)
 #pragma unroll
         for (int r = 0; r < S; ++r) a.per_source[(size_t)h * S + r] = sep[r];

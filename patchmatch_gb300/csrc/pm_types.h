@@ -1,6 +1,7 @@
 // Internal types shared by the host code and the kernels.
 #pragma once
 
+#include <cuda_runtime.h>
 #include <stdint.h>
 
 #include "pm_gb300.h"
@@ -10,10 +11,10 @@ namespace pm {
 constexpr int kMaxSrc = PM_MAX_SOURCES;
 
 // Composed reference-camera -> source-camera poses, FP64-composed on the
-// host and rounded to float: X_r = M_r X_c + c_r.
+// host and rounded to float: X_r = M_r X_c + c_r, stored as three rows
+// (M_r[k][0..2], c_r[k]) per source so a row is one 16-byte load.
 struct PmPoses {
-    float M[kMaxSrc][9];
-    float c[kMaxSrc][3];
+    float4 G[kMaxSrc][3];
 };
 
 // Per-source sampling images: quad-packed footprints (exact sampler) or
@@ -49,6 +50,17 @@ struct SweepArgs {
     float ncf, ndf;             // -log2(e) * color_factor, -log2(e) * dist_factor
     float depth_range[6];       // refinement depth ranges 0.02 * 0.3^t (float, reference rounding)
     float normal_range[6];      // refinement normal ranges 0.5 * 0.8^t
+};
+
+static_assert(sizeof(SweepArgs) % 16 == 0, "SweepArgs is copied as 16-byte words");
+
+// Arguments of the batched executor (one phase over many requests).
+struct BatchArgs {
+    const SweepArgs *args;   // per request (mode/colour/sweep taken from here)
+    const int4 *items;       // (request, tile x, tile y, 0), request-major
+    int n_items;
+    unsigned int *counter;   // next item; zero before the launch
+    int mode, colour, sweep;
 };
 
 // kModeScore: score each pixel's own plane; kModeSweep: red-black update;

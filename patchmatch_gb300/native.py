@@ -18,6 +18,7 @@ SEAM_CLAMP, SEAM_WRAP = 0, 1
 INIT_LOGUNIFORM_HEMI, INIT_REF_UNIFORM = 0, 1
 IMAGE_U8, IMAGE_F16 = 0, 1
 SAMPLER_EXACT, SAMPLER_TEXTURE = 0, 1
+BATCH_PERSISTENT, BATCH_LAUNCHES, BATCH_STREAMS = 0, 1, 2
 PROPAGATION_SMOOTH, PROPAGATION_PLAIN = 0, 1
 ORDER_BGR, ORDER_RGB = 0, 1
 MAX_SOURCES = 10
@@ -28,6 +29,8 @@ EXPORTS = (
     "pm_stream", "pm_probe_fp32_peak",
     "pm_densify", "pm_request_create", "pm_request_destroy", "pm_request_bytes", "pm_request_set_params",
     "pm_request_set_view", "pm_request_init", "pm_request_set_state", "pm_request_sweep", "pm_request_postprocess",
+    "pm_batch_create", "pm_batch_add", "pm_batch_clear", "pm_batch_set_executor", "pm_batch_run",
+    "pm_batch_synchronize", "pm_batch_stream", "pm_batch_tune", "pm_batch_destroy",
     "pm_score_view", "pm_depth_interval", "pm_write_ply", "pm_write_dense_msgpack",
     "pm_image_to_gray", "pm_image_resize", "pm_build_pyramid_f16",
     "pm_request_seed", "pm_request_set_prior", "pm_request_set_landmarks", "pm_request_seed_landmarks", "pm_result_bytes", "pm_result_create", "pm_result_snapshot",
@@ -67,6 +70,10 @@ class ServerConfig(C.Structure):
                 ("min_sources", C.c_int), ("max_sources", C.c_int), ("min_baseline", C.c_float),
                 ("max_baseline", C.c_float), ("seed_from_prior", C.c_int), ("seeded_iterations", C.c_int),
                 ("prior_lag", C.c_int), ("poll_us", C.c_int)]
+
+
+class BatchTuning(C.Structure):
+    _fields_ = [("executor", C.c_int), ("grid_mult", C.c_int), ("ms", C.c_float), ("candidate_ms", C.c_float * 4)]
 
 
 class ServedInfo(C.Structure):
@@ -129,6 +136,14 @@ def lib():
     L.pm_fuse.argtypes = [_vp, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, C.c_float, _vp, C.POINTER(Points)]
     L.pm_fuse_noalloc.argtypes = [C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, C.c_float, _vp, _vp, _vp, _vp, _vp,
                                   _vp]
+    L.pm_batch_create.argtypes = [_vp, C.POINTER(_vp)]
+    for f in ("pm_batch_clear", "pm_batch_run", "pm_batch_synchronize", "pm_batch_destroy"):
+        getattr(L, f).argtypes = [_vp]
+    L.pm_batch_add.argtypes = [_vp, _vp]
+    L.pm_batch_set_executor.argtypes = [_vp, C.c_int, C.c_int]
+    L.pm_batch_stream.restype = _vp
+    L.pm_batch_stream.argtypes = [_vp]
+    L.pm_batch_tune.argtypes = [_vp, C.POINTER(BatchTuning)]
     L.pm_score_view.argtypes = [_vp, _vp, _vp, C.c_int, _vp, _vp, C.c_int, C.POINTER(C.c_float),
                                 C.POINTER(C.c_int)]
     L.pm_depth_interval.argtypes = [_vp, _vp, _vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
@@ -519,6 +534,58 @@ class Result:
     def close(self):
         if getattr(self, "h", None):
             self._L.pm_result_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """The batched executor (pm_batch) over requests of one context."""
+
+    def __init__(self, ctx: Context, requests=()):
+        self.ctx = ctx
+        self._L = ctx._L
+        h = C.c_void_p()
+        ctx.check(self._L.pm_batch_create(ctx.h, C.byref(h)))
+        self.h = h.value
+        self.requests = []
+        for r in requests:
+            self.add(r)
+
+    def add(self, req: "Request"):
+        self.ctx.check(self._L.pm_batch_add(self.h, req.h))
+        self.requests.append(req)
+
+    def clear(self):
+        self.ctx.check(self._L.pm_batch_clear(self.h))
+        self.requests = []
+
+    def set_executor(self, executor: int, grid_mult: int = 1):
+        self.ctx.check(self._L.pm_batch_set_executor(self.h, executor, grid_mult))
+
+    def run(self):
+        self.ctx.check(self._L.pm_batch_run(self.h))
+
+    def synchronize(self):
+        self.ctx.check(self._L.pm_batch_synchronize(self.h))
+
+    @property
+    def stream_handle(self) -> int:
+        return int(self._L.pm_batch_stream(self.h))
+
+    def tune(self) -> dict:
+        t = BatchTuning()
+        self.ctx.check(self._L.pm_batch_tune(self.h, C.byref(t)))
+        return {"executor": t.executor, "grid_mult": t.grid_mult, "ms": t.ms,
+                "candidate_ms": list(t.candidate_ms)}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._L.pm_batch_destroy(self.h)
             self.h = None
 
     def __del__(self):

@@ -1,0 +1,86 @@
+"""The batched executor (pm_batch): requests of uneven size, source count,
+sampler and propagation rule densified together give exactly the maps of
+pm_request_run, whichever executor runs them."""
+import numpy as np
+import pytest
+
+from patchmatch_gb300 import native, scene
+
+pytestmark = pytest.mark.gpu
+
+SPECS = [  # (W, H, sources, seed, extra params)
+    (256, 128, 2, 1, {}),
+    (384, 192, 3, 2, {}),
+    (256, 128, 2, 3, {}),
+    (320, 160, 4, 4, {"sampler": native.SAMPLER_EXACT}),
+    (192, 96, 3, 5, {"propagation": native.PROPAGATION_PLAIN}),
+    (512, 256, 5, 6, {"iterations": 3}),
+]
+
+
+@pytest.fixture(scope="module")
+def batch_requests():
+    return [scene.make_request(scene.ROOM_OBJECTS, W, H, S, seed=seed) for W, H, S, seed, _ in SPECS]
+
+
+def _make(ctx, reqs):
+    out = []
+    for (W, H, S, seed, extra), req in zip(SPECS, reqs):
+        kw = {"iterations": 2, **extra}
+        p = native.default_params(seed=seed, keyframe_id=seed, **kw)
+        r = ctx.request(W, H, S, p)
+        r.set_views([v.gray_u8 for v in req.views], req.R, req.t)
+        out.append(r)
+    return out
+
+
+def test_batch_equals_individual_runs(ctx, batch_requests):
+    rs = _make(ctx, batch_requests)
+    alone = []
+    for r in rs:
+        r.run()
+        alone.append(r.read(want=("depth", "score", "plane")))
+    b = native.Batch(ctx, rs)
+    for executor, mult in ((native.BATCH_PERSISTENT, 1), (native.BATCH_PERSISTENT, 2), (native.BATCH_LAUNCHES, 1),
+                           (native.BATCH_STREAMS, 1)):
+        b.set_executor(executor, mult)
+        b.run()
+        for r, a in zip(rs, alone):
+            got = r.read(want=("depth", "score", "plane"))
+            for k in ("depth", "score", "plane"):
+                assert np.array_equal(got[k], a[k]), (executor, mult, k, r.W, r.S)
+    t = b.tune()
+    print("tuning:", t)
+    assert t["executor"] in (native.BATCH_PERSISTENT, native.BATCH_LAUNCHES, native.BATCH_STREAMS) and t["ms"] > 0
+    b.run()
+    assert np.array_equal(rs[1].read(want=("depth",))["depth"], alone[1]["depth"])
+    # new views (another scene, other poses) on a request: every executor follows
+    other = scene.make_request(scene.ROOM, 256, 128, 2, seed=9)
+    rs[0].set_views([v.gray_u8 for v in other.views], other.R, other.t)
+    rs[0].run()
+    solo = rs[0].read(want=("depth",))["depth"]
+    for executor in (native.BATCH_PERSISTENT, native.BATCH_LAUNCHES, native.BATCH_STREAMS):
+        b.set_executor(executor, 1)
+        b.run()
+        assert np.array_equal(rs[0].read(want=("depth",))["depth"], solo), executor
+    b.close()
+    for r in rs:
+        r.close()
+
+
+def test_batch_rejects_seeded_requests(ctx, batch_requests):
+    rs = _make(ctx, batch_requests[:2])
+    rs[0].run()
+    rs[1].set_prior(rs[0])
+    b = native.Batch(ctx, rs)
+    with pytest.raises(native.PmError) as e:
+        b.run()
+    assert e.value.status == native.PM_EINVAL
+    rs[1].set_prior(None)
+    b.run()
+    b.synchronize()
+    with pytest.raises(native.PmError):
+        b.add(rs[0])  # already in the batch
+    b.close()
+    for r in rs:
+        r.close()
