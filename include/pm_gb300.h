@@ -395,17 +395,18 @@ int pm_batch_destroy(pm_batch *b);
  * pm_image_resize: bilinear resize of 1-4 interleaved u8 channels, pixel
  *   centres aligned, 11-bit fixed-point weights, one rounding (cv::resize's
  *   linear scheme for thumbnails and masks).
- * pm_build_pyramid_f16: out[0] = the u8 image as FP16 (W x H, tightly
- *   packed), out[k] = 2x2 means of out[k-1] ((w+1)/2 x (h+1)/2, the last
- *   row/column repeated at odd sizes), summed in FP32 and rounded once. */
+ * pm_build_pyramid_f16: out[0] = the image (u8 or FP16 per src_format) as
+ *   FP16 (W x H, tightly packed; may be the FP16 source itself), out[k] =
+ *   2x2 means of out[k-1] ((w+1)/2 x (h+1)/2, the last row/column repeated
+ *   at odd sizes), summed in FP32 and rounded once. */
 #define PM_ORDER_BGR 0
 #define PM_ORDER_RGB 1
 int pm_image_to_gray(pm_ctx *ctx, const void *src, int width, int height, size_t pitch, int channels, int order,
                      void *gray, size_t gray_pitch);
 int pm_image_resize(pm_ctx *ctx, const void *src, int src_w, int src_h, size_t src_pitch, int channels, void *dst,
                     int dst_w, int dst_h, size_t dst_pitch);
-int pm_build_pyramid_f16(pm_ctx *ctx, const void *src, int width, int height, size_t pitch, int levels,
-                         void *const *out);
+int pm_build_pyramid_f16(pm_ctx *ctx, const void *src, int width, int height, size_t pitch, int src_format,
+                         int levels, void *const *out);
 
 /* ---- dense map output (host) ----
  * pm_write_ply: the fused points as ASCII PLY (x y z in fixed notation,

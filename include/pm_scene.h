@@ -82,6 +82,11 @@ int pm_scene_render_device(const pm_scene *s, const double R[9], const double t[
                            float noise_sigma, uint32_t noise_seed, uint8_t *gray_u8, float *depth, uint8_t *bgr,
                            void *stream);
 
+/* The unrounded intensities (0..255 scale, noise added) of the device
+ * renderer as H*W floats, for FP16 image studies. */
+int pm_scene_render_device_f32(const pm_scene *s, const double R[9], const double t[3], int W, int H,
+                               int supersample, float noise_sigma, uint32_t noise_seed, float *gray, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -107,12 +107,22 @@ int pm_image_resize(pm_ctx *ctx, const void *src, int sw, int sh, size_t spitch,
     return cudaGetLastError() == cudaSuccess ? PM_OK : PM_ECUDA;
 }
 
-int pm_build_pyramid_f16(pm_ctx *ctx, const void *src, int W, int H, size_t pitch, int levels, void *const *out) {
-    if (!ctx || !src || !out || W < 1 || H < 1 || levels < 1 || levels > 16 || pitch < (size_t)W) return PM_EINVAL;
+int pm_build_pyramid_f16(pm_ctx *ctx, const void *src, int W, int H, size_t pitch, int src_format, int levels,
+                         void *const *out) {
+    const size_t es = src_format == PM_IMAGE_F16 ? 2 : 1;
+    if (!ctx || !src || !out || W < 1 || H < 1 || levels < 1 || levels > 16 || pitch < (size_t)W * es ||
+        (src_format != PM_IMAGE_U8 && src_format != PM_IMAGE_F16))
+        return PM_EINVAL;
     for (int k = 0; k < levels; ++k)
         if (!out[k]) return PM_EINVAL;
     cudaStream_t st = (cudaStream_t)pm_stream(ctx);
-    u8_to_half_kernel<<<grid2(W, H), dim3(32, 8), 0, st>>>((const uint8_t *)src, W, H, pitch, (__half *)out[0]);
+    if (src_format == PM_IMAGE_U8) {
+        u8_to_half_kernel<<<grid2(W, H), dim3(32, 8), 0, st>>>((const uint8_t *)src, W, H, pitch, (__half *)out[0]);
+    } else if (out[0] != src || pitch != (size_t)W * 2) {
+        if (cudaMemcpy2DAsync(out[0], (size_t)W * 2, src, pitch, (size_t)W * 2, H, cudaMemcpyDeviceToDevice, st) !=
+            cudaSuccess)
+            return PM_ECUDA;
+    }
     int w = W, h = H;
     for (int k = 1; k < levels; ++k) {
         const int dw = (w + 1) / 2, dh = (h + 1) / 2;

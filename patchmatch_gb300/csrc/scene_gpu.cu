@@ -100,7 +100,7 @@ __device__ float intersect(const DevScene &s, const float o[3], const float d[3]
 }
 
 __global__ void render_kernel(const DevScene s, int W, int H, int ss, float noise_sigma, uint32_t noise_seed,
-                              uint8_t *gray, float *depth, uint8_t *bgr) {
+                              uint8_t *gray, float *depth, uint8_t *bgr, float *grayf) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= H || j >= W) return;
     const float kPi = 3.14159265358979323846f;
@@ -134,6 +134,7 @@ __global__ void render_kernel(const DevScene s, int W, int H, int ss, float nois
         g += noise_sigma * sqrtf(-2.0f * logf(u1)) * cosf(2.0f * kPi * u2);
     }
     if (gray) gray[idx] = (uint8_t)fminf(255.f, fmaxf(0.f, floorf(g + 0.5f)));
+    if (grayf) grayf[idx] = g;
     if (bgr)
         for (int c = 0; c < 3; ++c)
             bgr[3 * idx + c] = (uint8_t)fminf(255.f, floorf(255.0f * accc[2 - c] / (ss * ss) + 0.5f));
@@ -141,9 +142,10 @@ __global__ void render_kernel(const DevScene s, int W, int H, int ss, float nois
 
 }  // namespace
 
-extern "C" int pm_scene_render_device(const pm_scene *sc, const double R[9], const double t[3], int W, int H,
-                                      int supersample, float noise_sigma, uint32_t noise_seed, uint8_t *gray,
-                                      float *depth, uint8_t *bgr, void *stream) {
+namespace {
+int render_device(const pm_scene *sc, const double R[9], const double t[3], int W, int H, int supersample,
+                  float noise_sigma, uint32_t noise_seed, uint8_t *gray, float *depth, uint8_t *bgr, float *grayf,
+                  void *stream) {
     pm_scene_desc d;
     if (!sc || W <= 0 || H <= 0 || supersample < 1 || pm_scene_describe(sc, &d)) return 1;
     DevScene s{};
@@ -167,6 +169,20 @@ extern "C" int pm_scene_render_device(const pm_scene *sc, const double R[9], con
     for (int a = 0; a < 3; ++a) s.C[a] = (float)(-(R[a] * t[0] + R[3 + a] * t[1] + R[6 + a] * t[2]));
     dim3 blk(16, 16), grd((W + 15) / 16, (H + 15) / 16);
     render_kernel<<<grd, blk, 0, (cudaStream_t)stream>>>(s, W, H, supersample, noise_sigma, noise_seed, gray, depth,
-                                                         bgr);
+                                                         bgr, grayf);
     return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+}  // namespace
+
+extern "C" int pm_scene_render_device(const pm_scene *sc, const double R[9], const double t[3], int W, int H,
+                                      int supersample, float noise_sigma, uint32_t noise_seed, uint8_t *gray,
+                                      float *depth, uint8_t *bgr, void *stream) {
+    return render_device(sc, R, t, W, H, supersample, noise_sigma, noise_seed, gray, depth, bgr, nullptr, stream);
+}
+
+extern "C" int pm_scene_render_device_f32(const pm_scene *sc, const double R[9], const double t[3], int W, int H,
+                                          int supersample, float noise_sigma, uint32_t noise_seed, float *gray,
+                                          void *stream) {
+    return render_device(sc, R, t, W, H, supersample, noise_sigma, noise_seed, nullptr, nullptr, nullptr, gray,
+                         stream);
 }

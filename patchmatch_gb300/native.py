@@ -150,7 +150,7 @@ def lib():
                                     C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.pm_image_to_gray.argtypes = [_vp, _vp, C.c_int, C.c_int, _sz, C.c_int, C.c_int, _vp, _sz]
     L.pm_image_resize.argtypes = [_vp, _vp, C.c_int, C.c_int, _sz, C.c_int, _vp, C.c_int, C.c_int, _sz]
-    L.pm_build_pyramid_f16.argtypes = [_vp, _vp, C.c_int, C.c_int, _sz, C.c_int, _vp]
+    L.pm_build_pyramid_f16.argtypes = [_vp, _vp, C.c_int, C.c_int, _sz, C.c_int, C.c_int, _vp]
     L.pm_write_ply.argtypes = [C.c_char_p, C.POINTER(Points)]
     L.pm_write_dense_msgpack.argtypes = [C.c_char_p, C.POINTER(Points), C.c_uint64, C.c_uint32]
     L.pm_server_config_default.argtypes = [C.POINTER(ServerConfig)]
@@ -323,16 +323,18 @@ class Context:
         return out
 
     def pyramid_f16(self, img, levels: int = 3):
-        """FP16 pyramid of a (H, W) uint8 CUDA tensor: list of float16 tensors."""
+        """FP16 pyramid of a (H, W) uint8 or float16 CUDA tensor: list of float16 tensors."""
         import torch
         img = img.contiguous()
         H, W = img.shape
+        f16 = img.dtype == torch.float16
         outs, w, h = [], W, H
         for _ in range(levels):
             outs.append(torch.empty((h, w), dtype=torch.float16, device=img.device))
             w, h = (w + 1) // 2, (h + 1) // 2
         arr = (C.c_void_p * levels)(*[o.data_ptr() for o in outs])
-        self.check(self._L.pm_build_pyramid_f16(self.h, img.data_ptr(), W, H, W, levels, arr))
+        self.check(self._L.pm_build_pyramid_f16(self.h, img.data_ptr(), W, H, W * (2 if f16 else 1),
+                                                IMAGE_F16 if f16 else IMAGE_U8, levels, arr))
         return outs
 
     def probe_fp32_peak(self) -> float:

@@ -36,6 +36,9 @@ def _lib():
         lib.pm_scene_render_device.restype = C.c_int
         lib.pm_scene_render_device.argtypes = [C.c_void_p, _dp, _dp, C.c_int, C.c_int, C.c_int, C.c_float,
                                                C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        lib.pm_scene_render_device_f32.restype = C.c_int
+        lib.pm_scene_render_device_f32.argtypes = [C.c_void_p, _dp, _dp, C.c_int, C.c_int, C.c_int, C.c_float,
+                                                   C.c_uint32, C.c_void_p, C.c_void_p]
         lib.pm_scene_render.restype = C.c_int
         lib.pm_scene_render.argtypes = [C.c_void_p, _dp, _dp, C.c_int, C.c_int, C.c_int, C.c_float,
                                         C.c_uint32, _fp, _u8p, _u8p, _fp, _fp]
@@ -100,6 +103,16 @@ class Scene:
                                               noise_seed, p(gray), p(depth), p(bgr), stream)
         if rc:
             raise RuntimeError("pm_scene_render_device failed")
+
+    def render_device_f32(self, R, t, W: int, H: int, gray, supersample: int = 2, noise_sigma: float = 0.0,
+                          noise_seed: int = 0, stream: int = 0):
+        """Unrounded intensities (float32 CUDA tensor (H, W)) on the GPU."""
+        R = np.ascontiguousarray(R, np.float64)
+        t = np.ascontiguousarray(t, np.float64)
+        rc = self._lib.pm_scene_render_device_f32(self._h, _ptr(R, _dp), _ptr(t, _dp), W, H, supersample, noise_sigma,
+                                                  noise_seed, gray.data_ptr(), stream)
+        if rc:
+            raise RuntimeError("pm_scene_render_device_f32 failed")
 
     def render(self, R, t, W: int, H: int, supersample: int = 2, noise_sigma: float = 0.0,
                noise_seed: int = 0) -> View:
