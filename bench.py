@@ -168,6 +168,28 @@ def cpu_sample(target_s: float = 12.0, threads: int = 0):
     return value, rows, secs, threads, V, req
 
 
+def reference_gpu_sweep_ms():
+    """The reference's own CUDA path (PatchMatchCuda.cu compiled unmodified,
+    launched with its launch shape and per-pass synchronisation) timed per
+    red+black sweep at 1920x960 with its two sources; None when the reference
+    kernels were not built or no GPU is present."""
+    try:
+        import torch
+        if not torch.cuda.is_available():
+            return None
+        from oracle import refkernels
+        if not refkernels.available():
+            return None
+        from patchmatch_gb300 import scene
+        req = scene.make_request(scene.ROOM_OBJECTS, W, H, 2, seed=33, bmin=0.1, bmax=0.8)
+        rk = refkernels.RefKernels()
+        rk.setup([v.gray_u8.astype(np.float32) for v in req.views], req.R, req.t)
+        rk.run(1, 0.3, 20.0)
+        return min(rk.time_passes(4) for _ in range(3))
+    except Exception:
+        return None
+
+
 def run_reference(args):
     rank, ws, _, dist = _dist()
     if rank != 0:
@@ -189,6 +211,14 @@ def run_reference(args):
                        "sample": sample},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    ref_gpu = None if args.no_reference_gpu else reference_gpu_sweep_ms()
+    if ref_gpu is not None:
+        # the reference's CUDA path supports exactly two sources: 8 sweeps of
+        # 1920x960 with 2 sources, as Mpix*views/s (sweeps only)
+        line["reference_cuda"] = {"ms_per_sweep": ref_gpu, "sources": 2, "W": W, "H": H,
+                                  "sweeps_value": (W * H / 1e6) * 2 / (SWEEPS * ref_gpu / 1e3), "unit": UNIT,
+                                  "note": "PatchMatchCuda.cu compiled unmodified for sm_103a, its launch shape and "
+                                          "per-pass device synchronisation; 2 sources (its only configuration)"}
     print(json.dumps(line))
 
 
@@ -437,6 +467,28 @@ def run_ours(args):
     m = dn > 0
     acc = float((np.abs(dn[m] - gt[m]) / gt[m] < 0.01).mean()) if m.any() else 0.0
 
+    # two sources (the reference CUDA path's only configuration), per red+black sweep
+    req2 = scene.make_request(scene.ROOM_OBJECTS, W, H, 2, seed=33, bmin=0.1, bmax=0.8)
+    r2 = ctx.request(W, H, 2, native.default_params(iterations=SWEEPS))
+    r2.set_views([v.gray_u8 for v in req2.views], req2.R, req2.t)
+    r2.run()
+    r2.synchronize()
+    st2 = torch.cuda.ExternalStream(r2.stream_handle)
+    two = []
+    for _ in range(3):
+        r2.init()
+        a2, b2 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(st2):
+            a2.record(st2)
+        r2.sweep(0, 2 * SWEEPS)
+        with torch.cuda.stream(st2):
+            b2.record(st2)
+        r2.synchronize()
+        two.append(a2.elapsed_time(b2) / SWEEPS)
+    r2.close()
+    two_source = {"ms_per_sweep": min(two), "sources": 2, "W": W, "H": H,
+                  "sweeps_value": (W * H / 1e6) * 2 / (SWEEPS * min(two) / 1e3), "unit": UNIT,
+                  "note": "compare with reference_cuda in the --impl reference line (same scene and sizes)"}
     served = None if args.no_served else run_served(native, scene, ctx, local, args)
     batched = None if args.no_batched else run_batched(native, scene, ctx, local, args)
     traffic = _traffic_from_profile()
@@ -467,6 +519,7 @@ def run_ours(args):
                          "launch_ms": sweep_ms, "traffic": traffic},
             "served": served,
             "batched": batched,
+            "two_source_sweeps": two_source,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "gpu_launches": int(gpu_launches),
@@ -489,6 +542,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-served", action="store_true", help="skip the served-form measurement")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-form measurement")
+    ap.add_argument("--no-reference-gpu", action="store_true",
+                    help="reference arm: skip timing the reference's CUDA path")
     ap.add_argument("--batched-requests", type=int, default=64, help="requests in the batched-form measurement")
     ap.add_argument("--served-rate", type=float, default=4.0, help="arrival rate of the capacity stream (Hz)")
     ap.add_argument("--served-seconds", type=float, default=30.0, help="length of the capacity stream (s)")
