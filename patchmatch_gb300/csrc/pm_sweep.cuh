@@ -42,14 +42,53 @@ __device__ __forceinline__ void load_tile(float4 *tile, const float2 *row_trig, 
     }
 }
 
-// Dynamic shared memory of tile_kernel: the staged tile only, so that most of
-// the SM's unified L1/shared storage stays L1 for the source-image samples.
-constexpr size_t kTileSmemBytes = sizeof(float4) * kTileRows * kTileCols;
+// While a hypothesis is scored, the rest of a pixel visit's state (current
+// and candidate planes, score, depths, reference moments, loop counters) is
+// parked in shared memory, one 4-byte slot per value and thread, so that the
+// scoring loop keeps its S accumulation chains in registers without spilling.
+constexpr int kParkSlots = 24;
+
+// Dynamic shared memory of tile_kernel: the staged tile and the parked state;
+// the rest of the SM's unified L1/shared storage stays L1 for the samples.
+constexpr size_t kTileSmemBytes = sizeof(float4) * kTileRows * kTileCols + sizeof(float) * kParkSlots * kThreads;
+
+// Per-thread slots of the parked state.  The accesses are volatile so that
+// the compiler does not keep the values in registers across the scoring loop.
+struct Park {
+    unsigned base;
+    __device__ __forceinline__ explicit Park(const float4 *tile)
+        : base((unsigned)__cvta_generic_to_shared(reinterpret_cast<const float *>(tile + kTileRows * kTileCols) +
+                                                  threadIdx.x)) {}
+    __device__ __forceinline__ void put(int k, float v) const {
+        asm volatile("st.shared.f32 [%0], %1;" ::"r"(base + 4u * kThreads * k), "f"(v) : "memory");
+    }
+    __device__ __forceinline__ float getf(int k) const {
+        float v;
+        asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(base + 4u * kThreads * k) : "memory");
+        return v;
+    }
+    __device__ __forceinline__ void put(int k, int v) const { put(k, __int_as_float(v)); }
+    __device__ __forceinline__ void put(int k, bool v) const { put(k, __int_as_float(v ? 1 : 0)); }
+    __device__ __forceinline__ void get(int k, float &v) const { v = getf(k); }
+    __device__ __forceinline__ void get(int k, int &v) const { v = __float_as_int(getf(k)); }
+    __device__ __forceinline__ void get(int k, bool &v) const { v = __float_as_int(getf(k)) != 0; }
+    template <class... T>
+    __device__ __forceinline__ void save(const T &...v) const {
+        int k = 0;
+        (put(k++, v), ...);
+    }
+    template <class... T>
+    __device__ __forceinline__ void load(T &...v) const {
+        int k = 0;
+        (get(k++, v), ...);
+    }
+};
 
 // Resident CTAs per SM the register allocation targets: 3 (80 registers)
-// keeps up to 6 sources spill-free; more sources need the 128-register budget.
+// holds up to 8 sources with the visit state parked; more sources need the
+// 128-register budget.
 template <int S>
-constexpr int tile_min_blocks() { return S <= 6 ? 3 : 2; }
+constexpr int tile_min_blocks() { return S <= 8 ? 3 : 2; }
 
 // Smoothness factor f in [0, 1] of a propagated plane p against the pixel's
 // current plane h and its depth before propagation (PatchMatchCuda.cu:322-337).
@@ -78,13 +117,14 @@ __device__ __forceinline__ void tile_body(const A &a, int bx, int by, float4 *ti
     __syncthreads();
 
     const int W = a.W, H = a.H, ph = a.patch_half;
-    const int i = i0 + ty;
+    int i = i0 + ty;
     const int p = (i + a.colour) & 1;
-    const int j = x0 + 2 * lane + p;
+    int j = x0 + 2 * lane + p;
     if (i < ph + 1 || i > H - ph - 1 || j < ph + 1 || j > W - ph - 1) return;  // PatchMatchCuda.cu:283
 
     const float4 ctr = tile[(ty + kHaloMax) * kTileCols + ((2 * lane + p + kHaloMax) >> 1)];
-    const float bxc = ctr.x, byc = ctr.y, bzc = ctr.z, Ic = ctr.w;
+    float bxc = ctr.x, byc = ctr.y, bzc = ctr.z;
+    const float Ic = ctr.w;
     const int nt = ph + 1;
     const int cbase = lane + ((kHaloMax - ph) >> 1);
     const int rbase = ty + kHaloMax - ph;
@@ -106,7 +146,7 @@ __device__ __forceinline__ void tile_body(const A &a, int bx, int by, float4 *ti
         }
     }
 
-    const size_t idx = (size_t)i * W + j;
+    size_t idx = (size_t)i * W + j;
     float4 cand = make_float4(0.f, 0.f, 0.f, 0.f);
     if (a.mode == kModeSeed) {
         cand = a.cand[idx];
@@ -118,7 +158,8 @@ __device__ __forceinline__ void tile_body(const A &a, int bx, int by, float4 *ti
     float score = a.score[idx];
     int best = a.best[idx];
     float hx = cur.x, hy = cur.y, hz = cur.z;   // plane_*_hyp of the reference
-    const float curr_depth = cur.w;
+    float curr_depth = cur.w;
+    float cand_w = cand.w;
     float cx = hx, cy = hy, cz = hz, current_depth = curr_depth;
     float depth_hyp = 0.f;
     const float shift = Img::shift_for(Ic);
@@ -204,6 +245,10 @@ __device__ __forceinline__ void tile_body(const A &a, int bx, int by, float4 *ti
         }
         if (!found) break;
 
+        const Park park(tile);
+        park.save(hx, hy, hz, cx, cy, cz, score, current_depth, depth_hyp, f, sw, swx, swxx, bxc, byc, bzc, curr_depth,
+                  cand_w, best, h, kr, moved, i, j);
+
         // ---- cost of hypothesis (px, py, pz) ----
         TapAccum<S, Img, Acc> acc;
         acc.zero();
@@ -222,6 +267,9 @@ __device__ __forceinline__ void tile_body(const A &a, int bx, int by, float4 *ti
                         xs);
             }
         }
+        park.load(hx, hy, hz, cx, cy, cz, score, current_depth, depth_hyp, f, sw, swx, swxx, bxc, byc, bzc, curr_depth,
+                  cand_w, best, h, kr, moved, i, j);
+        idx = (size_t)i * W + j;
         float sep[S], cum[S];
         source_nccs(acc, sw, swx, swxx, a.combine, sep, cum);
         int hb;
@@ -232,7 +280,7 @@ __device__ __forceinline__ void tile_body(const A &a, int bx, int by, float4 *ti
             best = hb;
         } else if (a.mode == kModeSeed) {
             if (sc > score) {  // the host seeding rule (depthmap.cc:483-487)
-                cx = px; cy = py; cz = pz; score = sc; current_depth = cand.w; best = hb;
+                cx = px; cy = py; cz = pz; score = sc; current_depth = cand_w; best = hb;
             }
         } else if (h < 8) {
             sc = __fmul_rn(sc, f);
