@@ -143,7 +143,16 @@ void pm_params_default(pm_params *p);
  * an HBM budget for admission (0 = 90 % of free memory).
  * Replaces the per-keyframe cudaMalloc/cudaFree of
  * DepthmapEstimator::ComputePatchMatch (depthmap.cc:557-800) and the global
- * constant-memory state of InitConstantMem (PatchMatchCuda.cu:885-912). */
+ * constant-memory state of InitConstantMem (PatchMatchCuda.cu:885-912).
+ *
+ * Threads and lifetimes: a context and everything made from it (requests,
+ * retained results, batches) are used from one host thread at a time; a
+ * pm_server works on its context from its own worker thread, so make no
+ * other calls on that context while the server exists.  Several contexts
+ * may run side by side.  A request added to a batch, and a request or
+ * retained result set as a prior, must stay alive until the batch is cleared
+ * or destroyed or the prior is replaced; destroy servers, batches, requests
+ * and results before their context. */
 int pm_create(int device, size_t hbm_budget_bytes, pm_ctx **out);
 int pm_destroy(pm_ctx *ctx);
 const char *pm_last_error(const pm_ctx *ctx);
