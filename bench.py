@@ -138,6 +138,20 @@ def _allmax(dist, x: float) -> float:
     return float(t.item())
 
 
+def _hbm_view(traffic, launch_ms):
+    """The same launch against the measured HBM copy bandwidth: DRAM bytes
+    (ncu) per launch over its CUDA-event time, to show it is not HBM-bound."""
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if traffic is None or not os.path.exists(path):
+        return None
+    peak = json.load(open(path)).get("hbm_gbs")
+    if not peak:
+        return None
+    gbs = traffic / (launch_ms * 1e-3) / 1e9
+    return {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"}
+
+
 def _traffic_from_profile():
     """DRAM bytes per sweep launch from the committed ncu summary, if any."""
     path = os.path.join(ROOT, "profiles", "tile_kernel_1920x960x6.md")
@@ -516,7 +530,8 @@ def run_ours(args):
                          "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                          "peak_source": "in-run FFMA probe (pm_probe_fp32_peak); MEASURED_PEAKS.json has no FP32 figure",
                          "flop_per_sample": FLOP_PER_SAMPLE, "samples_per_launch": _samples_per_half_sweep(),
-                         "launch_ms": sweep_ms, "traffic": traffic},
+                         "launch_ms": sweep_ms, "traffic": traffic,
+                         "hbm_view": _hbm_view(traffic, sweep_ms)},
             "served": served,
             "batched": batched,
             "two_source_sweeps": two_source,
