@@ -448,3 +448,47 @@ def test_plain_propagation_matches_oracle(ctx, room):
     print(f"plain full run: agreement {agree:.4f}, acc5% {acc:.4f}")
     assert agree >= 0.90
     r.close()
+
+
+def test_mask_postprocess_bit_exact(ctx, room):
+    """A reference-view mask (pm_view.mask, the reference's masks_[0]) drops
+    the masked pixels in the post-filter exactly as the oracle does."""
+    rng = np.random.default_rng(8)
+    mask = np.ones((H1, W1), np.uint8)
+    mask[:, W1 // 3:W1 // 2] = 0               # a band, like a masked tripod or robot
+    mask[rng.random((H1, W1)) < 0.05] = 0      # and scattered pixels
+    p = native.default_params(iterations=2, postprocess=1, sampler=native.SAMPLER_EXACT)
+    r = ctx.request(W1, H1, room.n_src, p)
+    r.set_views([v.gray_u8 for v in room.views], room.R, room.t, mask=mask)
+    r.run()
+    raw = r.read(raw=True)
+    filt = r.read(raw=False)
+    d, s = O.postprocess(room.views[0].gray_u8.astype(np.float32), raw["depth"], raw["score"], mask=mask)
+    assert np.array_equal(filt["depth"], d) and np.array_equal(filt["score"], s)
+    assert (filt["depth"][mask == 0] == 0).all()
+    assert (filt["depth"][mask == 1] > 0).mean() > 0.3
+    r.close()
+
+
+@pytest.mark.parametrize("patch_half", [1, 3])
+def test_smaller_windows_match_fp64_oracle(ctx, room, patch_half):
+    """Windows of 2x2 and 4x4 taps (PatchSize 3 and 5): per-source NCC within
+    1e-5 of the FP64 oracle for >= 99.5 % of fixed hypotheses with 16 taps and
+    >= 98.5 % with 4 (four samples put many variances near the 0.1 floor,
+    where FP32 rounding of the moments weighs most); all within 1e-3."""
+    ij, planes = _hypotheses(room, 5000, 9)
+    r = _req_on_gpu(ctx, room, patch_half=patch_half)
+    _, _, gps = r.score_hypotheses(ij, planes, per_source=True)
+    _, _, ops = O.cost_batch(O.Views.from_request(room), O.cost_params(patch_half=patch_half), ij, planes,
+                             want_ncc=True)
+    err = np.abs(gps - ops)
+    print(f"patch_half={patch_half}: median {np.median(err):.2e} p99.9 {np.quantile(err, .999):.2e}")
+    assert (err <= 1e-5 * np.maximum(1, np.abs(ops))).mean() >= (0.995 if patch_half == 3 else 0.985)
+    assert np.quantile(err, 0.999) <= 1e-4 and (err <= 1e-3).mean() >= 0.9999
+    # a full run at this window size completes and is reproducible
+    r.set_params(native.default_params(iterations=2, patch_half=patch_half, sampler=native.SAMPLER_EXACT))
+    r.run()
+    a = r.read(want=("depth",))["depth"]
+    r.run()
+    assert np.array_equal(a, r.read(want=("depth",))["depth"]) and (a > 0).mean() > 0.2
+    r.close()
