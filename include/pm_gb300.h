@@ -319,6 +319,10 @@ typedef struct {
     double queue_ms;         /* submit -> start on the GPU */
     double latency_ms;       /* submit -> maps on the host */
 } pm_served_info;
+/* Memory: requests and retained results (20 B/px, at most prior_lag + 1 per
+ * image size) are admitted against the context's HBM budget; the keyframe
+ * cache (cache_capacity images of W*H bytes) and pinned host buffers for the
+ * results are allocated outside it, once, and reused. */
 void pm_server_config_default(pm_server_config *cfg);
 int pm_server_create(pm_ctx *ctx, const pm_server_config *cfg, pm_server **out);
 /* Copies the keyframe's gray image (uint8) and pose; returns a ticket. */
