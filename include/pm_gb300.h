@@ -310,11 +310,16 @@ typedef struct {
     int seeded_iterations;   /* sweeps of a seeded keyframe (2) */
     int prior_lag;           /* seed from the newest densified keyframe at least this many back (4) */
     int poll_us;             /* worker polling interval while work is in flight */
+    int coarse_to_fine;      /* 1: a keyframe without a prior, at least 1920 wide with even sizes, is
+                                densified at half resolution first (params.iterations sweeps) and
+                                then refined at full resolution (seeded_iterations sweeps) seeded
+                                from that result */
 } pm_server_config;
 typedef struct {
     int status;              /* PM_OK, PM_ENOTREADY (too few neighbours) or an error */
     int n_sources;
-    int seeded;
+    int seeded;              /* 0: random initialisation, 1: an earlier keyframe's result,
+                                2: its own half-resolution pass (coarse_to_fine) */
     int iterations;
     double queue_ms;         /* submit -> start on the GPU */
     double latency_ms;       /* submit -> maps on the host */

@@ -69,7 +69,7 @@ class ServerConfig(C.Structure):
     _fields_ = [("params", Params), ("cache_capacity", C.c_int), ("max_inflight", C.c_int),
                 ("min_sources", C.c_int), ("max_sources", C.c_int), ("min_baseline", C.c_float),
                 ("max_baseline", C.c_float), ("seed_from_prior", C.c_int), ("seeded_iterations", C.c_int),
-                ("prior_lag", C.c_int), ("poll_us", C.c_int)]
+                ("prior_lag", C.c_int), ("poll_us", C.c_int), ("coarse_to_fine", C.c_int)]
 
 
 class BatchTuning(C.Structure):

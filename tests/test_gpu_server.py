@@ -98,3 +98,48 @@ def test_device_renderer_matches_host_renderer(built):
     assert np.abs(dd - host.depth).max() / host.depth.max() < 1e-4
     gg = g.cpu().numpy().astype(int)
     assert np.mean(np.abs(gg - host.gray_u8.astype(int))) < 1.0
+
+
+def test_coarse_to_fine_start(ctx):
+    """Keyframes without a prior (the start of a stream) at 1920x960 run
+    coarse to fine: the configured sweeps at half resolution, then the seeded
+    sweep count at full resolution.  Their results stay independent of the
+    mix and are about as accurate as the configured sweeps at full
+    resolution, in less time."""
+    import torch
+    sc = scene.Scene(scene.HALL, 21)
+    Wc, Hc = 1920, 960
+    g = torch.empty((Hc, Wc), dtype=torch.uint8, device="cuda")
+    dd = torch.empty((Hc, Wc), dtype=torch.float32, device="cuda")
+    views = []
+    for k in range(6):
+        R, t = sc.trajectory_pose(3, 20, 60.0, 2.0 + 0.5 * k)
+        sc.render_device(R, t, Wc, Hc, gray=g, depth=dd)
+        torch.cuda.synchronize()
+        views.append((g.cpu().numpy(), dd.cpu().numpy(), R, t))
+    p = native.default_params(iterations=8)
+    res = {}
+    for c2f in (0, 1):
+        cfg = native.server_config(params=p, max_inflight=4, min_sources=2, max_sources=4, prior_lag=4,
+                                   seeded_iterations=2, min_baseline=0.02, max_baseline=3.0, coarse_to_fine=c2f)
+        srv = native.Server(ctx, cfg)
+        tks = [srv.submit(im, R, t) for im, _, R, t in views]
+        res[c2f] = [srv.wait(tk) for tk in tks]
+        srv.close()
+    first = next(k for k, r in enumerate(res[1]) if r[0] == native.PM_OK)
+    assert res[1][first][3]["seeded"] == 2 and res[0][first][3]["seeded"] == 0
+    assert res[1][first][3]["iterations"] == 2
+    gt = views[first][1]
+    acc = lambda d: (np.abs(d - gt) / gt < 0.01)[d > 0].mean()
+    a0, a1 = acc(res[0][first][1]), acc(res[1][first][1])
+    print(f"first densified keyframe {first}: 8 sweeps acc1% {a0:.4f}, coarse-to-fine {a1:.4f}")
+    assert a1 >= a0 - 0.02
+    cfg = native.server_config(params=p, max_inflight=1, min_sources=2, max_sources=4, prior_lag=4,
+                               seeded_iterations=2, min_baseline=0.02, max_baseline=3.0)
+    srv = native.Server(ctx, cfg)
+    alone = [srv.wait(srv.submit(im, R, t)) for im, _, R, t in views]
+    srv.close()
+    for k in range(len(views)):
+        assert alone[k][0] == res[1][k][0]
+        if alone[k][0] == native.PM_OK:
+            assert np.array_equal(alone[k][1], res[1][k][1]), k
