@@ -16,7 +16,8 @@ keyframe (whole job: summed over GPUs; N > 1 runs independent replicas).
 served: the same densifier behind the served request loop (pm_server) on a
           keyframe stream along a trajectory through a hall of boxes, mixed
           1920x960 / 3840x1920 keyframes, 4-8 neighbours from a 40-keyframe
-          device cache, prior results reused as initialisation; capacity
+          device cache, prior results reused as initialisation (keyframes
+          without one start coarse to fine); capacity
           (stream submitted at once) against the plain form on the same
           stream (one keyframe at a time, no prior, 8 sweeps), and p50/p99
           latency of 1920x960 keyframes with 6 neighbours arriving as a
