@@ -215,7 +215,10 @@ cudaEvent_t get_event(pm_server *s) {
         return e;
     }
     cudaEvent_t e = nullptr;
-    cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
     return e;
 }
 
@@ -431,8 +434,15 @@ int start_job(pm_server *s, Submission &sub, CachedKeyframe *kf) {
             std::memcpy(v.t_cw, c->t, sizeof v.t_cw);
             const int e = pm_request_set_view(r, k, &v);
             if (e) return e;
-            b->uses.push_back(get_event(s));
-            cudaEventRecord(b->uses.back(), rs);
+            // the buffer is reused only after this event: a use that cannot be
+            // recorded fails the keyframe (its request is synchronised then)
+            cudaEvent_t u = get_event(s);
+            if (!u || cudaEventRecord(u, rs) != cudaSuccess) {
+                cudaGetLastError();
+                if (u) s->event_pool.push_back(u);
+                return PM_ECUDA;
+            }
+            b->uses.push_back(u);
         }
         return PM_OK;
     };
