@@ -512,7 +512,7 @@ def run_ours(args):
     line = None
     if rank == 0:
         cpu = None
-        if not args.no_cpu:
+        if not args.no_cpu and ws == 1:  # the CPU leg runs at N = 1 only
             v, rows, secs, threads, _, _ = cpu_sample(target_s=args.cpu_seconds)
             cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                    "sample": f"{rows} rows x 1920 of the same workload, all {SWEEPS} sweeps, "
