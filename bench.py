@@ -383,7 +383,8 @@ def run_batched(native, scene, ctx, local: int, args) -> dict:
     batch_s = e0.elapsed_time(e1) / 1e3
     b.close()
     names = {native.BATCH_PERSISTENT: "persistent tile queue", native.BATCH_LAUNCHES: "per-request launches",
-             native.BATCH_STREAMS: "parallel graph branches"}
+             native.BATCH_STREAMS: "parallel graph branches",
+             native.BATCH_MIXED: "one persistent tile queue over all source counts"}
     for r in reqs:
         r.close()
     return {"requests": len(reqs), "work_mpix_views": work,
@@ -393,7 +394,7 @@ def run_batched(native, scene, ctx, local: int, args) -> dict:
                         "gpu_launches": int(l1 - l0), "clocks": clk.summary()},
             "ratio_batched_over_plain": plain_s / batch_s,
             "tuning_ms_first16": dict(zip(["persistent x1", "persistent x2", "per-request launches",
-                                           "parallel graph branches"], tuning["candidate_ms"])),
+                                           "parallel graph branches", "mixed persistent"], tuning["candidate_ms"])),
             "workload": f"{len(reqs)} requests, sizes uniform over {[f'{w}x{h}' for w, h in BATCH_SIZES]}, 3-10 "
                         f"sources, room scenes with per-request seeds, {SWEEPS} sweeps; results bit-identical "
                         "between the forms"}

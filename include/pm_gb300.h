@@ -375,7 +375,10 @@ int pm_fuse_noalloc(int width, int height, int n_views, float *const *depths, co
  * items (PM_BATCH_PERSISTENT, grid = grid_mult x resident CTAs) or one launch
  * per request (PM_BATCH_LAUNCHES); PM_BATCH_STREAMS instead runs each
  * request's whole chain on one of 8 parallel graph branches (largest request
- * first onto the least-loaded branch) so that requests overlap on the GPU.  Every request's maps equal those of
+ * first onto the least-loaded branch) so that requests overlap on the GPU;
+ * PM_BATCH_MIXED is one persistent launch per phase over all requests of
+ * every source count (items carry their count; the kernel holds the bodies
+ * of all counts, at the register budget of the largest).  Every request's maps equal those of
  * pm_request_run bit for bit.  Requests keep their own buffers and streams:
  * set their views before pm_batch_run; read them afterwards with
  * pm_request_read (their streams wait for the batch).  Seeding (priors,
@@ -386,11 +389,14 @@ int pm_fuse_noalloc(int width, int height, int n_views, float *const *depths, co
 #define PM_BATCH_PERSISTENT 0
 #define PM_BATCH_LAUNCHES 1
 #define PM_BATCH_STREAMS 2
+#define PM_BATCH_MIXED 3
+#define PM_BATCH_CANDIDATES 5
 typedef struct {
     int executor;            /* chosen PM_BATCH_* */
     int grid_mult;           /* chosen persistent grid multiple */
     float ms;                /* its time for one pm_batch_run */
-    float candidate_ms[4];   /* persistent x1, persistent x2, per-request launches, parallel branches */
+    float candidate_ms[PM_BATCH_CANDIDATES];  /* persistent x1, persistent x2, per-request launches,
+                                                 parallel branches, mixed persistent */
 } pm_batch_tuning;
 int pm_batch_create(pm_ctx *ctx, pm_batch **out);
 int pm_batch_add(pm_batch *b, pm_request *req);

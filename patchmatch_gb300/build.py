@@ -48,6 +48,9 @@ def _sources():
     # the cost/sweep kernels flush subnormals to zero: no value on that path is
     # subnormal, and it keeps the approximate reciprocal/rsqrt/exp2 single
     # instructions (NaN handling is unaffected)
+    for k in range(4):  # the batched executor's mixed kernel, one unit per image variant
+        units.append((os.path.join(CSRC, "pm_batch_mixed.cu"), os.path.join(OBJ_DIR, f"pm_batch_mixed_k{k}.o"),
+                      [f"-DPM_MIXED_KIND={k}", "-ftz=true"]))
     for s in range(1, MAX_SOURCES + 1):
         units.append((os.path.join(CSRC, "pm_inst.cu"), os.path.join(OBJ_DIR, f"pm_inst_s{s}.o"),
                       [f"-DPM_INST_S={s}", "-ftz=true"]))

@@ -549,6 +549,24 @@ cudaError_t dispatch_batch(int S, int kind, bool plain, int blocks, cudaStream_t
     }
 }
 
+cudaError_t dispatch_batch_mixed(int kind, bool plain, int blocks, cudaStream_t st, const BatchArgs &b) {
+    switch (kind) {
+        case kImageQuadF16: return launch_batch_mixed<kImageQuadF16>(plain, blocks, st, b);
+        case kImageTexU8: return launch_batch_mixed<kImageTexU8>(plain, blocks, st, b);
+        case kImageTexF16: return launch_batch_mixed<kImageTexF16>(plain, blocks, st, b);
+        default: return launch_batch_mixed<kImageQuadU8>(plain, blocks, st, b);
+    }
+}
+
+int dispatch_batch_mixed_blocks_per_sm(int kind, bool plain) {
+    switch (kind) {
+        case kImageQuadF16: return batch_mixed_blocks_per_sm<kImageQuadF16>(plain);
+        case kImageTexU8: return batch_mixed_blocks_per_sm<kImageTexU8>(plain);
+        case kImageTexF16: return batch_mixed_blocks_per_sm<kImageTexF16>(plain);
+        default: return batch_mixed_blocks_per_sm<kImageQuadU8>(plain);
+    }
+}
+
 int dispatch_batch_blocks_per_sm(int S, int kind, bool plain) {
     switch (S) {
         case 1: return batch_blocks_per_sm<1>(kind, plain);
@@ -1428,12 +1446,14 @@ int batch_build(pm_batch *b) {
         const int kind = pm::image_kind(r->prm.image_format, r->prm.sampler);
         const bool plain = r->prm.propagation == PM_PROPAGATION_PLAIN;
         pm_batch::Group *g = nullptr;
+        // the mixed kernel takes every source count in one group (S = 0)
+        const int gS = b->executor == PM_BATCH_MIXED ? 0 : r->S;
         for (auto &x : b->groups)
-            if (x.S == r->S && x.kind == kind && x.plain == plain && x.iterations == r->prm.iterations) g = &x;
+            if (x.S == gS && x.kind == kind && x.plain == plain && x.iterations == r->prm.iterations) g = &x;
         if (!g) {
             b->groups.emplace_back();
             g = &b->groups.back();
-            g->S = r->S;
+            g->S = gS;
             g->kind = kind;
             g->plain = plain;
             g->iterations = r->prm.iterations;
@@ -1445,7 +1465,7 @@ int batch_build(pm_batch *b) {
         for (int m = 0; m < (int)g.members.size(); ++m) {
             const dim3 tg = pm::tile_grid(g.members[m]->W, g.members[m]->H);
             for (unsigned y = 0; y < tg.y; ++y)
-                for (unsigned x = 0; x < tg.x; ++x) items.push_back(make_int4(m, (int)x, (int)y, 0));
+                for (unsigned x = 0; x < tg.x; ++x) items.push_back(make_int4(m, (int)x, (int)y, g.members[m]->S));
         }
         g.n_items = (int)items.size();
         g.n_phases = 2 + 2 * g.iterations;
@@ -1529,7 +1549,7 @@ int batch_enqueue(pm_batch *b) {
         const int sweep = ph < 2 ? 0 : (ph - 2) >> 1;
         for (auto &g : b->groups) {
             if (ph >= g.n_phases) continue;
-            if (b->executor == PM_BATCH_PERSISTENT) {
+            if (b->executor == PM_BATCH_PERSISTENT || b->executor == PM_BATCH_MIXED) {
                 pm::BatchArgs a{};
                 a.args = g.d_args;
                 a.items = g.d_items;
@@ -1538,9 +1558,12 @@ int batch_enqueue(pm_batch *b) {
                 a.mode = mode;
                 a.colour = colour;
                 a.sweep = sweep;
-                const int occ = std::max(1, pm::dispatch_batch_blocks_per_sm(g.S, g.kind, g.plain));
+                const bool mixed = b->executor == PM_BATCH_MIXED;
+                const int occ = std::max(1, mixed ? pm::dispatch_batch_mixed_blocks_per_sm(g.kind, g.plain)
+                                                  : pm::dispatch_batch_blocks_per_sm(g.S, g.kind, g.plain));
                 const int blocks = std::max(1, std::min(g.n_items, b->grid_mult * occ * sms));
-                cudaError_t e = pm::dispatch_batch(g.S, g.kind, g.plain, blocks, st, a);
+                cudaError_t e = mixed ? pm::dispatch_batch_mixed(g.kind, g.plain, blocks, st, a)
+                                      : pm::dispatch_batch(g.S, g.kind, g.plain, blocks, st, a);
                 if (e != cudaSuccess) return fail(ctx, PM_ECUDA, "batch launch: %s", cudaGetErrorString(e));
                 ++launches;
             } else {
@@ -1618,7 +1641,7 @@ int pm_batch_clear(pm_batch *b) {
 }
 
 int pm_batch_set_executor(pm_batch *b, int executor, int grid_mult) {
-    if (!b || executor < PM_BATCH_PERSISTENT || executor > PM_BATCH_STREAMS || grid_mult < 1 || grid_mult > 16)
+    if (!b || executor < PM_BATCH_PERSISTENT || executor > PM_BATCH_MIXED || grid_mult < 1 || grid_mult > 16)
         return PM_EINVAL;
     if (executor != b->executor || grid_mult != b->grid_mult) b->dirty = true;
     b->executor = executor;
@@ -1648,7 +1671,7 @@ int pm_batch_run(pm_batch *b) {
         sig.insert(sig.end(), p2, p2 + sizeof r->prm);
     }
     for (pm_request *r : b->reqs) fill_args(r);
-    if (b->executor != PM_BATCH_PERSISTENT)  // per-request launches bake the arguments (poses) in
+    if (b->executor == PM_BATCH_LAUNCHES || b->executor == PM_BATCH_STREAMS)  // launches bake the poses in
         for (pm_request *r : b->reqs) {
             const char *p3 = reinterpret_cast<const char *>(&r->args);
             sig.insert(sig.end(), p3, p3 + sizeof r->args);
@@ -1714,14 +1737,14 @@ int pm_batch_tune(pm_batch *b, pm_batch_tuning *out) {
     if (!b) return PM_EINVAL;
     pm_ctx *ctx = b->ctx;
     const int cand[][2] = {{PM_BATCH_PERSISTENT, 1}, {PM_BATCH_PERSISTENT, 2}, {PM_BATCH_LAUNCHES, 1},
-                           {PM_BATCH_STREAMS, 1}};
+                           {PM_BATCH_STREAMS, 1}, {PM_BATCH_MIXED, 1}};
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     PM_CUDA(ctx, cudaEventCreate(&e0));
     PM_CUDA(ctx, cudaEventCreate(&e1));
     float best_ms = 1e30f;
     int best = 0;
     int rc = PM_OK;
-    for (int c = 0; c < 4 && !rc; ++c) {
+    for (int c = 0; c < PM_BATCH_CANDIDATES && !rc; ++c) {
         pm_batch_set_executor(b, cand[c][0], cand[c][1]);
         rc = pm_batch_run(b);  // builds the graph (untimed)
         float ms = 0.f;

@@ -33,6 +33,13 @@ template <int S>
 cudaError_t launch_batch(int kind, bool plain, int blocks, cudaStream_t st, const BatchArgs &b);
 template <int S>
 int batch_blocks_per_sm(int kind, bool plain);
+// pm_batch_mixed.cu (one translation unit per image variant)
+template <int Kind>
+cudaError_t launch_batch_mixed(bool plain, int blocks, cudaStream_t st, const BatchArgs &b);
+template <int Kind>
+int batch_mixed_blocks_per_sm(bool plain);
+cudaError_t dispatch_batch_mixed(int kind, bool plain, int blocks, cudaStream_t st, const BatchArgs &b);
+int dispatch_batch_mixed_blocks_per_sm(int kind, bool plain);
 cudaError_t dispatch_tile(int S, int kind, dim3 grid, cudaStream_t st, const SweepArgs &a);
 cudaError_t dispatch_batch(int S, int kind, bool plain, int blocks, cudaStream_t st, const BatchArgs &b);
 int dispatch_batch_blocks_per_sm(int S, int kind, bool plain);

@@ -18,7 +18,7 @@ SEAM_CLAMP, SEAM_WRAP = 0, 1
 INIT_LOGUNIFORM_HEMI, INIT_REF_UNIFORM = 0, 1
 IMAGE_U8, IMAGE_F16 = 0, 1
 SAMPLER_EXACT, SAMPLER_TEXTURE = 0, 1
-BATCH_PERSISTENT, BATCH_LAUNCHES, BATCH_STREAMS = 0, 1, 2
+BATCH_PERSISTENT, BATCH_LAUNCHES, BATCH_STREAMS, BATCH_MIXED = 0, 1, 2, 3
 PROPAGATION_SMOOTH, PROPAGATION_PLAIN = 0, 1
 ORDER_BGR, ORDER_RGB = 0, 1
 MAX_SOURCES = 10
@@ -73,7 +73,7 @@ class ServerConfig(C.Structure):
 
 
 class BatchTuning(C.Structure):
-    _fields_ = [("executor", C.c_int), ("grid_mult", C.c_int), ("ms", C.c_float), ("candidate_ms", C.c_float * 4)]
+    _fields_ = [("executor", C.c_int), ("grid_mult", C.c_int), ("ms", C.c_float), ("candidate_ms", C.c_float * 5)]
 
 
 class ServedInfo(C.Structure):

@@ -42,7 +42,7 @@ def test_batch_equals_individual_runs(ctx, batch_requests):
         alone.append(r.read(want=("depth", "score", "plane")))
     b = native.Batch(ctx, rs)
     for executor, mult in ((native.BATCH_PERSISTENT, 1), (native.BATCH_PERSISTENT, 2), (native.BATCH_LAUNCHES, 1),
-                           (native.BATCH_STREAMS, 1)):
+                           (native.BATCH_STREAMS, 1), (native.BATCH_MIXED, 1)):
         b.set_executor(executor, mult)
         b.run()
         for r, a in zip(rs, alone):
@@ -51,7 +51,8 @@ def test_batch_equals_individual_runs(ctx, batch_requests):
                 assert np.array_equal(got[k], a[k]), (executor, mult, k, r.W, r.S)
     t = b.tune()
     print("tuning:", t)
-    assert t["executor"] in (native.BATCH_PERSISTENT, native.BATCH_LAUNCHES, native.BATCH_STREAMS) and t["ms"] > 0
+    assert t["executor"] in (native.BATCH_PERSISTENT, native.BATCH_LAUNCHES, native.BATCH_STREAMS,
+                             native.BATCH_MIXED) and t["ms"] > 0
     b.run()
     assert np.array_equal(rs[1].read(want=("depth",))["depth"], alone[1]["depth"])
     # new views (another scene, other poses) on a request: every executor follows
@@ -59,7 +60,7 @@ def test_batch_equals_individual_runs(ctx, batch_requests):
     rs[0].set_views([v.gray_u8 for v in other.views], other.R, other.t)
     rs[0].run()
     solo = rs[0].read(want=("depth",))["depth"]
-    for executor in (native.BATCH_PERSISTENT, native.BATCH_LAUNCHES, native.BATCH_STREAMS):
+    for executor in (native.BATCH_PERSISTENT, native.BATCH_LAUNCHES, native.BATCH_STREAMS, native.BATCH_MIXED):
         b.set_executor(executor, 1)
         b.run()
         assert np.array_equal(rs[0].read(want=("depth",))["depth"], solo), executor
