@@ -492,3 +492,13 @@ def test_smaller_windows_match_fp64_oracle(ctx, room, patch_half):
     r.run()
     assert np.array_equal(a, r.read(want=("depth",))["depth"]) and (a > 0).mean() > 0.2
     r.close()
+
+
+def test_size_limits_are_rejected(ctx):
+    """Sizes beyond the supported range fail with PM_EINVAL before any device
+    work: wider than 32768, taller than 16384, or a (W+1)(H+1) sampling grid
+    of 2^31 entries or more."""
+    for W, H in ((32769, 64), (64, 16385), (32768, 65536), (15, 64), (64, 15)):
+        with pytest.raises(native.PmError) as e:
+            ctx.request(W, H, 2, native.default_params())
+        assert e.value.status == native.PM_EINVAL, (W, H)
