@@ -323,6 +323,40 @@ def run_served(native, scene, ctx, local: int, args) -> dict:
     return out
 
 
+def run_pipeline(native, scene, ctx, local: int, steps: int) -> dict:
+    """The stages after densification at 1920x960 over a 5-keyframe window
+    (the reference's cleaner and pruner queues): geometric-consistency filter
+    (pm_filter_consistency) and point fusion (pm_fuse), each timed through the
+    C ABI with host buffers in and out (copies included)."""
+    import torch
+    sc = scene.Scene(scene.ROOM_OBJECTS, 14)
+    R, t = sc.poses(5, 14, 0.1, 0.4, 15.0)
+    d = torch.empty((H, W), dtype=torch.float32, device=f"cuda:{local}")
+    rgb = torch.empty((H, W, 3), dtype=torch.uint8, device=f"cuda:{local}")
+    rng = np.random.default_rng(0)
+    depths = []
+    for v in range(5):
+        sc.render_device(R[v], t[v], W, H, depth=d, bgr=rgb if v == 0 else None)
+        torch.cuda.synchronize()
+        dv = d.cpu().numpy() * (1 + rng.normal(0, 0.004, (H, W))).astype(np.float32)
+        dv[rng.random((H, W)) < 0.1] = 0
+        depths.append(dv.astype(np.float32))
+    bgr = rgb.cpu().numpy()
+    out = {}
+    for name, fn in (("filter", lambda: ctx.filter_consistency(depths, R, t, center=2, thr=0.01, min_consistent=3)),
+                     ("fuse", lambda: ctx.fuse(depths, R, t, bgr, 0.02))):
+        fn()
+        ts = []
+        for _ in range(max(3, steps)):
+            t0 = time.perf_counter()
+            fn()
+            ts.append(time.perf_counter() - t0)
+        out[f"{name}_ms"] = 1e3 * statistics.median(ts)
+    out["workload"] = ("1920x960, 5 depth maps (0.4 % noise, 10 % holes); filter: centre map 2, 1 % depth "
+                       "threshold, 3 consistent views; fuse: head map 0 against 1-4, 2 % threshold; host buffers")
+    return out
+
+
 BATCH_SIZES = ((960, 480), (1920, 960), (2880, 1440), (3840, 1920))
 
 
@@ -509,6 +543,7 @@ def run_ours(args):
                   "note": "compare with reference_cuda in the --impl reference line (same scene and sizes)"}
     served = None if args.no_served else run_served(native, scene, ctx, local, args)
     batched = None if args.no_batched else run_batched(native, scene, ctx, local, args)
+    pipeline = run_pipeline(native, scene, ctx, local, args.steps)
     traffic = _traffic_from_profile()
     line = None
     if rank == 0:
@@ -538,6 +573,7 @@ def run_ours(args):
                          "hbm_view": _hbm_view(traffic, sweep_ms)},
             "served": served,
             "batched": batched,
+            "pipeline": pipeline,
             "two_source_sweeps": two_source,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
