@@ -341,19 +341,43 @@ def run_pipeline(native, scene, ctx, local: int, steps: int) -> dict:
         dv = d.cpu().numpy() * (1 + rng.normal(0, 0.004, (H, W))).astype(np.float32)
         dv[rng.random((H, W)) < 0.1] = 0
         depths.append(dv.astype(np.float32))
-    bgr = rgb.cpu().numpy()
+    bgr = np.ascontiguousarray(rgb.cpu().numpy())
+    import ctypes as C
+    L = native.lib()
+    Rd = np.ascontiguousarray(R, np.float64)
+    td = np.ascontiguousarray(t, np.float64)
+    work = [d.copy() for d in depths]          # pm_fuse edits the later maps in place
+    ptrs = (C.c_void_p * 5)(*[w.ctypes.data for w in work])
+    cleaned = np.zeros((H, W), np.float32)
+    pruned = np.zeros((H, W), np.float32)
+    xyz = np.zeros((H * W, 3), np.float64)
+    cols = np.zeros((H * W, 3), np.uint8)
+    ij = np.zeros((H * W, 2), np.int32)
+    pts = native.Points(H * W, 0, xyz.ctypes.data, cols.ctypes.data, ij.ctypes.data)
+
+    def clean():
+        ctx.check(L.pm_filter_consistency(ctx.h, W, H, 5, C.cast(ptrs, C.c_void_p), Rd.ctypes.data, td.ctypes.data,
+                                          2, 0.01, 3, 0.0, cleaned.ctypes.data))
+
+    def fuse():
+        ctx.check(L.pm_fuse(ctx.h, W, H, 5, C.cast(ptrs, C.c_void_p), Rd.ctypes.data, td.ctypes.data,
+                            bgr.ctypes.data, 0.02, pruned.ctypes.data, C.byref(pts)))
+
     out = {}
-    for name, fn in (("filter", lambda: ctx.filter_consistency(depths, R, t, center=2, thr=0.01, min_consistent=3)),
-                     ("fuse", lambda: ctx.fuse(depths, R, t, bgr, 0.02))):
-        fn()
+    for name, fn in (("filter", clean), ("fuse", fuse)):
         ts = []
-        for _ in range(max(3, steps)):
+        for k in range(max(3, steps) + 1):
+            for w, d0 in zip(work, depths):
+                np.copyto(w, d0)               # fresh maps, outside the timed call
             t0 = time.perf_counter()
             fn()
-            ts.append(time.perf_counter() - t0)
+            if k:
+                ts.append(time.perf_counter() - t0)
         out[f"{name}_ms"] = 1e3 * statistics.median(ts)
+    out["fused_points"] = int(pts.count)
     out["workload"] = ("1920x960, 5 depth maps (0.4 % noise, 10 % holes); filter: centre map 2, 1 % depth "
-                       "threshold, 3 consistent views; fuse: head map 0 against 1-4, 2 % threshold; host buffers")
+                       "threshold, 3 consistent views; fuse: head map 0 against 1-4, 2 % threshold; one C ABI "
+                       "call each with host buffers in and out (copies included, buffers preallocated)")
     return out
 
 
