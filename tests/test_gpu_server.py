@@ -143,3 +143,31 @@ def test_coarse_to_fine_start(ctx):
         assert alone[k][0] == res[1][k][0]
         if alone[k][0] == native.PM_OK:
             assert np.array_equal(alone[k][1], res[1][k][1]), k
+
+
+def test_mixed_sizes_alone_and_in_the_mix(ctx):
+    """Keyframes of two sizes in one stream: neighbours and priors are taken
+    from keyframes of the same size only, and every result is the same
+    whether the keyframes run one at a time or overlapped."""
+    sc = scene.Scene(scene.ROOM_OBJECTS, 62)
+    views = []
+    for k in range(12):
+        Wk, Hk = (384, 192) if k % 3 else (512, 256)
+        R, t = sc.trajectory_pose(6, 8, 12.0, 0.5 + 0.25 * k)
+        views.append(sc.render(R, t, Wk, Hk))
+    out = {}
+    for inflight in (1, 4):
+        srv = native.Server(ctx, _cfg(inflight))
+        tks = [srv.submit(v.gray_u8, v.R, v.t) for v in views]
+        out[inflight] = [srv.wait(tk) for tk in tks]
+        srv.close()
+    dense = 0
+    for k, v in enumerate(views):
+        a, b = out[1][k], out[4][k]
+        assert a[0] == b[0] and a[3]["n_sources"] == b[3]["n_sources"] and a[3]["seeded"] == b[3]["seeded"], k
+        if a[0] == native.PM_OK:
+            dense += 1
+            assert a[1].shape == v.gray_u8.shape and np.array_equal(a[1], b[1]), k
+            n_same = sum(1 for j in range(k) if views[j].gray_u8.shape == v.gray_u8.shape)
+            assert a[3]["n_sources"] <= n_same
+    assert dense >= 6
