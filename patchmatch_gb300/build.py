@@ -43,7 +43,7 @@ def _sources():
     deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     deps += [os.path.join(INC, f) for f in os.listdir(INC)]
     units = []
-    for f in ("pm_api.cu", "pm_prep.cu", "pm_post.cu", "pm_seed.cu", "pm_input.cu", "pm_fuse_noalloc.cu", "pm_dense.cpp", "pm_server.cpp", "pm_views.cpp", "pm_io.cpp"):
+    for f in ("pm_api.cu", "pm_batch.cu", "pm_prep.cu", "pm_post.cu", "pm_seed.cu", "pm_input.cu", "pm_fuse_noalloc.cu", "pm_dense.cpp", "pm_server.cpp", "pm_views.cpp", "pm_io.cpp"):
         units.append((os.path.join(CSRC, f), os.path.join(OBJ_DIR, os.path.splitext(f)[0] + ".o"), []))
     # the cost/sweep kernels flush subnormals to zero: no value on that path is
     # subnormal, and it keeps the approximate reciprocal/rsqrt/exp2 single

@@ -1,6 +1,7 @@
 // C ABI of the densifier (include/pm_gb300.h): contexts, device-resident
 // requests, the captured init/sweep/post-filter graph, fixed-hypothesis
-// scoring, the consistency filter and point fusion.
+// scoring, the consistency filter and point fusion.  The batched executor
+// is in pm_batch.cu.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -12,6 +13,7 @@
 #include <vector>
 
 #include "pm_gb300.h"
+#include "pm_internal.h"
 #include "pm_kernels.h"
 #include "pm_sweep.cuh"
 
@@ -19,6 +21,12 @@ namespace pm {
 template <int S>
 cudaError_t configure_tile();
 }
+
+using pmi::fail;
+using pmi::align256;
+using pmi::fill_args;
+using pmi::check_views;
+using pmi::enqueue_post;
 
 namespace {
 
@@ -36,99 +44,13 @@ __global__ void fp32_probe_kernel(float *out, int iters, float a, float b) {
     if (s == 1.2345f) out[0] = s;  // keeps the chains alive
 }
 
-struct Trig {
-    int W = 0, H = 0;
-    float2 *row = nullptr, *col = nullptr;
-};
-
 }  // namespace
-
-struct pm_ctx {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    size_t budget = 0, used = 0;
-    std::string err;
-    uint64_t launches = 0;
-    std::vector<Trig> trig;
-    pm_request *cached = nullptr;
-    void *scratch = nullptr;
-    size_t scratch_bytes = 0;
-};
-
-struct pm_request {
-    pm_ctx *ctx = nullptr;
-    int W = 0, H = 0, S = 0;
-    pm_params prm{};
-    size_t bytes = 0;
-    void *block = nullptr;  // one device allocation holding everything below
-    float *ref = nullptr;
-    uint8_t *raw = nullptr;
-    void *quad[PM_MAX_SOURCES] = {};     // quad-packed footprints, or pitched images for textures
-    cudaTextureObject_t tex[PM_MAX_SOURCES] = {};
-    int tex_format = -1;                 // image format the texture objects were made for (-1: none)
-    size_t tex_pitch = 0;
-    uint8_t *mask = nullptr;
-    bool has_mask = false;
-    float4 *plane = nullptr;
-    float *score = nullptr;
-    int8_t *best = nullptr;
-    float *d0 = nullptr, *s0 = nullptr, *m1 = nullptr, *fdepth = nullptr, *fscore = nullptr;
-    float *x_depth = nullptr, *x_score = nullptr, *x_plane3 = nullptr, *x_normal3 = nullptr;
-    int32_t *x_best = nullptr;
-    float4 *seed = nullptr;              // seeding candidates from a prior result
-    unsigned long long *zbuf = nullptr;  // splat depth test of the prior warp
-    const pm_request *prior = nullptr;   // result reused as initialisation (may be null)
-    const pm_result *prior_res = nullptr;
-    int2 *lm = nullptr;                  // landmark seeds (pixel index, depth bits), device
-    int n_lm = 0, lm_cap = 0;
-    double R[PM_MAX_SOURCES + 1][9] = {}, t[PM_MAX_SOURCES + 1][3] = {};
-    bool have[PM_MAX_SOURCES + 1] = {};
-    Trig trig;
-    pm::SweepArgs args{};
-    cudaStream_t stream = nullptr;  // the request's own stream: requests overlap on the device
-    cudaEvent_t ready = nullptr;    // recorded on this stream for requests seeded from it
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t gexec = nullptr;
-    bool graph_dirty = true;
-    bool postprocessed = false;
-};
-
-// A retained keyframe result (plane state + filtered depth + pose): the
-// compact form in which results are kept for seeding later keyframes.
-struct pm_result {
-    pm_ctx *ctx = nullptr;
-    int W = 0, H = 0;
-    size_t bytes = 0;
-    void *block = nullptr;
-    float4 *plane = nullptr;
-    float *fdepth = nullptr;
-    double R[9] = {}, t[3] = {};
-    Trig trig;
-    cudaEvent_t ready = nullptr;  // recorded after the snapshot copies
-    bool valid = false;
-};
 
 namespace {
 
-int fail(pm_ctx *ctx, int code, const char *fmt, ...) {
-    if (ctx) {
-        char buf[512];
-        va_list ap;
-        va_start(ap, fmt);
-        vsnprintf(buf, sizeof buf, fmt, ap);
-        va_end(ap);
-        ctx->err = buf;
-    }
-    return code;
-}
 
-#define PM_CUDA(ctx, call)                                                                             \
-    do {                                                                                               \
-        cudaError_t e_ = (call);                                                                       \
-        if (e_ != cudaSuccess) return fail((ctx), PM_ECUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
-    } while (0)
 
-size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
 
 int __float_as_int_host(float f) {
     int i;
@@ -231,7 +153,9 @@ int validate_size(pm_ctx *ctx, int W, int H, int S) {
     return PM_OK;
 }
 
-void fill_args(pm_request *r) {
+}  // namespace
+
+void pmi::fill_args(pm_request *r) {
     pm::SweepArgs &a = r->args;
     const pm_params &p = r->prm;
     for (int k = 0; k < r->S; ++k) {
@@ -272,6 +196,8 @@ void fill_args(pm_request *r) {
         nr = (float)(nr * 0.8);
     }
 }
+
+namespace {
 
 void destroy_textures(pm_request *r) {
     for (int k = 0; k < r->S; ++k)
@@ -339,11 +265,15 @@ int launch_tile(pm_request *r, int mode, int colour, int sweep) {
     return PM_OK;
 }
 
-int check_views(pm_request *r) {
+}  // namespace
+
+int pmi::check_views(pm_request *r) {
     for (int k = 0; k <= r->S; ++k)
         if (!r->have[k]) return fail(r->ctx, PM_EINVAL, "view %d has not been set", k);
     return PM_OK;
 }
+
+namespace {
 
 int enqueue_init(pm_request *r) {
     const pm_params &p = r->prm;
@@ -365,7 +295,9 @@ int enqueue_sweeps(pm_request *r, int first_half, int n_half) {
     return PM_OK;
 }
 
-int enqueue_post(pm_request *r, cudaStream_t st = nullptr) {
+}  // namespace
+
+int pmi::enqueue_post(pm_request *r, cudaStream_t st) {
     pm::PostArgs a{};
     a.plane = r->plane;
     a.score = r->score;
@@ -390,6 +322,8 @@ int enqueue_post(pm_request *r, cudaStream_t st = nullptr) {
 
 // Splat the prior result into this keyframe and keep candidates that score
 // higher than the random initialisation.
+namespace {
+
 // Where a seeding prior comes from: a request's state or a retained result.
 struct PriorSrc {
     const float4 *plane;
@@ -1388,408 +1322,3 @@ int pm_fuse(pm_ctx *ctx, int W, int H, int n, float *const *depths, const double
 
 }  // extern "C"
 
-// ---------------------------------------------------------------------------
-// Batched executor: many requests densified by phase-major launches (init
-// scoring, then each red/black half-sweep of every request, then the
-// post-filter), captured once into a CUDA graph and replayed.  Requests are
-// grouped by (source count, image variant, propagation rule, sweep count);
-// each phase of a group is one persistent launch over a device queue of
-// (request, tile) items (PM_BATCH_PERSISTENT) or one launch per request
-// (PM_BATCH_LAUNCHES).  A tile's update reads only pixels of the other colour,
-// so the result of every request is the same as from pm_request_run.
-// ---------------------------------------------------------------------------
-struct pm_batch {
-    struct Group {
-        int S = 0, kind = 0, iterations = 0;
-        bool plain = false;
-        std::vector<pm_request *> members;
-        pm::SweepArgs *d_args = nullptr;
-        int4 *d_items = nullptr;
-        int n_items = 0;
-        unsigned int *d_counters = nullptr;
-        int n_phases = 0;
-        std::vector<pm::SweepArgs> h_args;
-    };
-    pm_ctx *ctx = nullptr;
-    std::vector<pm_request *> reqs;
-    std::vector<Group> groups;
-    cudaStream_t stream = nullptr;
-    cudaEvent_t done = nullptr;
-    std::vector<cudaEvent_t> req_events;
-    static constexpr int kBranches = 8;      // PM_BATCH_STREAMS: parallel chains of requests
-    cudaStream_t branch[kBranches] = {};
-    cudaEvent_t fork = nullptr, join[kBranches] = {};
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t gexec = nullptr;
-    bool dirty = true;
-    std::vector<char> signature;   // what the captured graph depends on
-    int executor = PM_BATCH_PERSISTENT;
-    int grid_mult = 1;
-    uint64_t launches_per_run = 0;
-};
-
-namespace {
-
-void batch_free_groups(pm_batch *b) {
-    for (auto &g : b->groups) {
-        cudaFree(g.d_args);
-        cudaFree(g.d_items);
-        cudaFree(g.d_counters);
-    }
-    b->groups.clear();
-}
-
-int batch_build(pm_batch *b) {
-    pm_ctx *ctx = b->ctx;
-    batch_free_groups(b);
-    for (pm_request *r : b->reqs) {
-        const int kind = pm::image_kind(r->prm.image_format, r->prm.sampler);
-        const bool plain = r->prm.propagation == PM_PROPAGATION_PLAIN;
-        pm_batch::Group *g = nullptr;
-        // the mixed kernel takes every source count in one group (S = 0)
-        const int gS = b->executor == PM_BATCH_MIXED ? 0 : r->S;
-        for (auto &x : b->groups)
-            if (x.S == gS && x.kind == kind && x.plain == plain && x.iterations == r->prm.iterations) g = &x;
-        if (!g) {
-            b->groups.emplace_back();
-            g = &b->groups.back();
-            g->S = gS;
-            g->kind = kind;
-            g->plain = plain;
-            g->iterations = r->prm.iterations;
-        }
-        g->members.push_back(r);
-    }
-    for (auto &g : b->groups) {
-        std::vector<int4> items;
-        for (int m = 0; m < (int)g.members.size(); ++m) {
-            const dim3 tg = pm::tile_grid(g.members[m]->W, g.members[m]->H);
-            for (unsigned y = 0; y < tg.y; ++y)
-                for (unsigned x = 0; x < tg.x; ++x) items.push_back(make_int4(m, (int)x, (int)y, g.members[m]->S));
-        }
-        g.n_items = (int)items.size();
-        g.n_phases = 2 + 2 * g.iterations;
-        g.h_args.resize(g.members.size());
-        if (cudaMalloc(&g.d_args, g.members.size() * sizeof(pm::SweepArgs)) != cudaSuccess ||
-            cudaMalloc(&g.d_items, items.size() * sizeof(int4)) != cudaSuccess ||
-            cudaMalloc(&g.d_counters, g.n_phases * sizeof(unsigned int)) != cudaSuccess) {
-            cudaGetLastError();
-            return fail(ctx, PM_ENOMEM, "batch work queues");
-        }
-        PM_CUDA(ctx, cudaMemcpy(g.d_items, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice));
-    }
-    return PM_OK;
-}
-
-int batch_enqueue(pm_batch *b) {
-    pm_ctx *ctx = b->ctx;
-    const cudaStream_t st = b->stream;
-    int sms = 0;
-    PM_CUDA(ctx, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
-    uint64_t launches = 0;
-    int max_phases = 0;
-    for (auto &g : b->groups) {
-        PM_CUDA(ctx, cudaMemsetAsync(g.d_counters, 0, g.n_phases * sizeof(unsigned int), st));
-        max_phases = std::max(max_phases, g.n_phases);
-    }
-    if (b->executor == PM_BATCH_STREAMS) {
-        // each request's whole chain on one of the branch streams (largest
-        // first onto the least-loaded branch), branches forked from and
-        // joined back into the batch stream
-        std::vector<pm_request *> order = b->reqs;
-        std::sort(order.begin(), order.end(), [](const pm_request *x, const pm_request *y) {
-            return (double)x->W * x->H * x->S * (1 + x->prm.iterations) >
-                   (double)y->W * y->H * y->S * (1 + y->prm.iterations);
-        });
-        double load[pm_batch::kBranches] = {};
-        const int nb = std::min<int>(pm_batch::kBranches, (int)order.size());
-        PM_CUDA(ctx, cudaEventRecord(b->fork, st));
-        for (int k = 0; k < nb; ++k) PM_CUDA(ctx, cudaStreamWaitEvent(b->branch[k], b->fork, 0));
-        for (pm_request *r : order) {
-            int k = 0;
-            for (int q = 1; q < nb; ++q)
-                if (load[q] < load[k]) k = q;
-            load[k] += (double)r->W * r->H * r->S * (1 + r->prm.iterations);
-            const cudaStream_t bs = b->branch[k];
-            const pm_params &p = r->prm;
-            pm::launch_init_planes(bs, r->trig.row, r->trig.col, r->W, r->H, p.seed, p.keyframe_id, p.init_mode,
-                                   p.min_depth, p.max_depth, r->plane, r->score, r->best);
-            ++launches;
-            const int kind = pm::image_kind(p.image_format, p.sampler);
-            for (int ph = 0; ph < 2 + 2 * p.iterations; ++ph) {
-                pm::SweepArgs a = r->args;
-                a.mode = ph < 2 ? pm::kModeScore : pm::kModeSweep;
-                a.colour = ph < 2 ? ph : (ph - 2) & 1;
-                a.sweep = ph < 2 ? 0 : (ph - 2) >> 1;
-                cudaError_t e = pm::dispatch_tile(r->S, kind, pm::tile_grid(r->W, r->H), bs, a);
-                if (e != cudaSuccess) return fail(ctx, PM_ECUDA, "tile launch: %s", cudaGetErrorString(e));
-                ++launches;
-            }
-            if (p.postprocess) {
-                enqueue_post(r, bs);
-                launches += 3;
-            }
-        }
-        for (int k = 0; k < nb; ++k) {
-            PM_CUDA(ctx, cudaEventRecord(b->join[k], b->branch[k]));
-            PM_CUDA(ctx, cudaStreamWaitEvent(st, b->join[k], 0));
-        }
-        b->launches_per_run = launches;
-        return PM_OK;
-    }
-    for (pm_request *r : b->reqs) {
-        const pm_params &p = r->prm;
-        pm::launch_init_planes(st, r->trig.row, r->trig.col, r->W, r->H, p.seed, p.keyframe_id, p.init_mode,
-                               p.min_depth, p.max_depth, r->plane, r->score, r->best);
-        ++launches;
-    }
-    for (int ph = 0; ph < max_phases; ++ph) {
-        const int mode = ph < 2 ? pm::kModeScore : pm::kModeSweep;
-        const int colour = ph < 2 ? ph : (ph - 2) & 1;
-        const int sweep = ph < 2 ? 0 : (ph - 2) >> 1;
-        for (auto &g : b->groups) {
-            if (ph >= g.n_phases) continue;
-            if (b->executor == PM_BATCH_PERSISTENT || b->executor == PM_BATCH_MIXED) {
-                pm::BatchArgs a{};
-                a.args = g.d_args;
-                a.items = g.d_items;
-                a.n_items = g.n_items;
-                a.counter = g.d_counters + ph;
-                a.mode = mode;
-                a.colour = colour;
-                a.sweep = sweep;
-                const bool mixed = b->executor == PM_BATCH_MIXED;
-                const int occ = std::max(1, mixed ? pm::dispatch_batch_mixed_blocks_per_sm(g.kind, g.plain)
-                                                  : pm::dispatch_batch_blocks_per_sm(g.S, g.kind, g.plain));
-                const int blocks = std::max(1, std::min(g.n_items, b->grid_mult * occ * sms));
-                cudaError_t e = mixed ? pm::dispatch_batch_mixed(g.kind, g.plain, blocks, st, a)
-                                      : pm::dispatch_batch(g.S, g.kind, g.plain, blocks, st, a);
-                if (e != cudaSuccess) return fail(ctx, PM_ECUDA, "batch launch: %s", cudaGetErrorString(e));
-                ++launches;
-            } else {
-                for (size_t m = 0; m < g.members.size(); ++m) {
-                    pm::SweepArgs a = g.h_args[m];
-                    a.mode = mode;
-                    a.colour = colour;
-                    a.sweep = sweep;
-                    cudaError_t e = pm::dispatch_tile(g.S, g.kind, pm::tile_grid(a.W, a.H), st, a);
-                    if (e != cudaSuccess) return fail(ctx, PM_ECUDA, "tile launch: %s", cudaGetErrorString(e));
-                    ++launches;
-                }
-            }
-        }
-    }
-    for (pm_request *r : b->reqs)
-        if (r->prm.postprocess) {
-            enqueue_post(r, st);
-            launches += 3;
-        }
-    b->launches_per_run = launches;
-    return PM_OK;
-}
-
-}  // namespace
-
-extern "C" {
-
-int pm_batch_create(pm_ctx *ctx, pm_batch **out) {
-    if (!ctx || !out) return PM_EINVAL;
-    *out = nullptr;
-    PM_CUDA(ctx, cudaSetDevice(ctx->device));
-    pm_batch *b = new pm_batch();
-    b->ctx = ctx;
-    bool ok = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) == cudaSuccess &&
-              cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming) == cudaSuccess &&
-              cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) == cudaSuccess;
-    for (int k = 0; ok && k < pm_batch::kBranches; ++k)
-        ok = cudaStreamCreateWithFlags(&b->branch[k], cudaStreamNonBlocking) == cudaSuccess &&
-             cudaEventCreateWithFlags(&b->join[k], cudaEventDisableTiming) == cudaSuccess;
-    if (!ok) {
-        cudaGetLastError();
-        pm_batch_destroy(b);
-        return fail(ctx, PM_ECUDA, "batch stream creation failed");
-    }
-    *out = b;
-    return PM_OK;
-}
-
-int pm_batch_add(pm_batch *b, pm_request *r) {
-    if (!b || !r) return PM_EINVAL;
-    if (r->ctx != b->ctx) return fail(b->ctx, PM_EINVAL, "request belongs to another context");
-    for (pm_request *q : b->reqs)
-        if (q == r) return fail(b->ctx, PM_EINVAL, "request already in the batch");
-    b->reqs.push_back(r);
-    cudaEvent_t e = nullptr;
-    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
-        cudaGetLastError();
-        b->reqs.pop_back();
-        return fail(b->ctx, PM_ECUDA, "event creation failed");
-    }
-    b->req_events.push_back(e);
-    b->dirty = true;
-    return PM_OK;
-}
-
-int pm_batch_clear(pm_batch *b) {
-    if (!b) return PM_EINVAL;
-    cudaStreamSynchronize(b->stream);
-    for (cudaEvent_t e : b->req_events) cudaEventDestroy(e);
-    b->req_events.clear();
-    b->reqs.clear();
-    b->dirty = true;
-    return PM_OK;
-}
-
-int pm_batch_set_executor(pm_batch *b, int executor, int grid_mult) {
-    if (!b || executor < PM_BATCH_PERSISTENT || executor > PM_BATCH_MIXED || grid_mult < 1 || grid_mult > 16)
-        return PM_EINVAL;
-    if (executor != b->executor || grid_mult != b->grid_mult) b->dirty = true;
-    b->executor = executor;
-    b->grid_mult = grid_mult;
-    return PM_OK;
-}
-
-int pm_batch_run(pm_batch *b) {
-    if (!b) return PM_EINVAL;
-    pm_ctx *ctx = b->ctx;
-    if (b->reqs.empty()) return fail(ctx, PM_EINVAL, "empty batch");
-    for (pm_request *r : b->reqs) {
-        int rc = check_views(r);
-        if (rc) return rc;
-        if (r->prior || r->prior_res || r->n_lm > 0)
-            return fail(ctx, PM_EINVAL, "batched requests are not seeded (clear the prior and landmarks)");
-    }
-    // the graph bakes in each request's shape, parameters and mask use
-    std::vector<char> sig;
-    for (pm_request *r : b->reqs) {
-        const char *p0 = reinterpret_cast<const char *>(&r);
-        sig.insert(sig.end(), p0, p0 + sizeof r);
-        const int shape[4] = {r->W, r->H, r->S, r->has_mask ? 1 : 0};
-        const char *p1 = reinterpret_cast<const char *>(shape);
-        sig.insert(sig.end(), p1, p1 + sizeof shape);
-        const char *p2 = reinterpret_cast<const char *>(&r->prm);
-        sig.insert(sig.end(), p2, p2 + sizeof r->prm);
-    }
-    for (pm_request *r : b->reqs) fill_args(r);
-    if (b->executor == PM_BATCH_LAUNCHES || b->executor == PM_BATCH_STREAMS)  // launches bake the poses in
-        for (pm_request *r : b->reqs) {
-            const char *p3 = reinterpret_cast<const char *>(&r->args);
-            sig.insert(sig.end(), p3, p3 + sizeof r->args);
-        }
-    const int ex[2] = {b->executor, b->grid_mult};
-    sig.insert(sig.end(), reinterpret_cast<const char *>(ex), reinterpret_cast<const char *>(ex) + sizeof ex);
-    if (sig != b->signature) b->dirty = true;
-    PM_CUDA(ctx, cudaSetDevice(ctx->device));
-    if (b->dirty || !b->gexec) {
-        int rc = batch_build(b);
-        if (rc) return rc;
-        cudaGraph_t g = nullptr;
-        for (auto &gr : b->groups)
-            for (size_t m = 0; m < gr.members.size(); ++m) gr.h_args[m] = gr.members[m]->args;
-        PM_CUDA(ctx, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-        const uint64_t before = ctx->launches;
-        rc = batch_enqueue(b);
-        cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
-        ctx->launches = before;
-        if (rc) {
-            if (g) cudaGraphDestroy(g);
-            return rc;
-        }
-        if (ce != cudaSuccess) return fail(ctx, PM_ECUDA, "batch graph capture: %s", cudaGetErrorString(ce));
-        if (b->gexec) cudaGraphExecDestroy(b->gexec);
-        if (b->graph) cudaGraphDestroy(b->graph);
-        b->gexec = nullptr;
-        b->graph = g;
-        PM_CUDA(ctx, cudaGraphInstantiate(&b->gexec, g, 0));
-        b->dirty = false;
-        b->signature = sig;
-    }
-    // the requests' own streams carry their uploads; the batch waits for them
-    for (size_t k = 0; k < b->reqs.size(); ++k) {
-        PM_CUDA(ctx, cudaEventRecord(b->req_events[k], b->reqs[k]->stream));
-        PM_CUDA(ctx, cudaStreamWaitEvent(b->stream, b->req_events[k], 0));
-    }
-    // per-request arguments (poses may have changed since the graph was built)
-    for (auto &g : b->groups) {
-        for (size_t m = 0; m < g.members.size(); ++m) g.h_args[m] = g.members[m]->args;
-        PM_CUDA(ctx, cudaMemcpyAsync(g.d_args, g.h_args.data(), g.h_args.size() * sizeof(pm::SweepArgs),
-                                     cudaMemcpyHostToDevice, b->stream));
-    }
-    PM_CUDA(ctx, cudaGraphLaunch(b->gexec, b->stream));
-    PM_CUDA(ctx, cudaEventRecord(b->done, b->stream));
-    for (pm_request *r : b->reqs) {
-        PM_CUDA(ctx, cudaStreamWaitEvent(r->stream, b->done, 0));
-        r->postprocessed = r->prm.postprocess != 0;
-    }
-    ctx->launches += b->launches_per_run;
-    return PM_OK;
-}
-
-int pm_batch_synchronize(pm_batch *b) {
-    if (!b) return PM_EINVAL;
-    PM_CUDA(b->ctx, cudaStreamSynchronize(b->stream));
-    return PM_OK;
-}
-
-void *pm_batch_stream(const pm_batch *b) { return b ? (void *)b->stream : nullptr; }
-
-int pm_batch_tune(pm_batch *b, pm_batch_tuning *out) {
-    if (!b) return PM_EINVAL;
-    pm_ctx *ctx = b->ctx;
-    const int cand[][2] = {{PM_BATCH_PERSISTENT, 1}, {PM_BATCH_PERSISTENT, 2}, {PM_BATCH_LAUNCHES, 1},
-                           {PM_BATCH_STREAMS, 1}, {PM_BATCH_MIXED, 1}};
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
-    PM_CUDA(ctx, cudaEventCreate(&e0));
-    PM_CUDA(ctx, cudaEventCreate(&e1));
-    float best_ms = 1e30f;
-    int best = 0;
-    int rc = PM_OK;
-    for (int c = 0; c < PM_BATCH_CANDIDATES && !rc; ++c) {
-        pm_batch_set_executor(b, cand[c][0], cand[c][1]);
-        rc = pm_batch_run(b);  // builds the graph (untimed)
-        float ms = 0.f;
-        if (!rc) {
-            cudaEventRecord(e0, b->stream);
-            rc = pm_batch_run(b);
-            cudaEventRecord(e1, b->stream);
-            if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
-                rc = fail(ctx, PM_ECUDA, "tuning timer");
-        }
-        if (!rc && out) out->candidate_ms[c] = ms;
-        if (!rc && ms < best_ms) {
-            best_ms = ms;
-            best = c;
-        }
-    }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    if (rc) return rc;
-    pm_batch_set_executor(b, cand[best][0], cand[best][1]);
-    if (out) {
-        out->executor = cand[best][0];
-        out->grid_mult = cand[best][1];
-        out->ms = best_ms;
-    }
-    return PM_OK;
-}
-
-int pm_batch_destroy(pm_batch *b) {
-    if (!b) return PM_EINVAL;
-    cudaSetDevice(b->ctx->device);
-    if (b->stream) cudaStreamSynchronize(b->stream);
-    if (b->gexec) cudaGraphExecDestroy(b->gexec);
-    if (b->graph) cudaGraphDestroy(b->graph);
-    batch_free_groups(b);
-    for (cudaEvent_t e : b->req_events) cudaEventDestroy(e);
-    for (int k = 0; k < pm_batch::kBranches; ++k) {
-        if (b->branch[k]) cudaStreamDestroy(b->branch[k]);
-        if (b->join[k]) cudaEventDestroy(b->join[k]);
-    }
-    if (b->fork) cudaEventDestroy(b->fork);
-    if (b->done) cudaEventDestroy(b->done);
-    if (b->stream) cudaStreamDestroy(b->stream);
-    delete b;
-    return PM_OK;
-}
-
-}  // extern "C"

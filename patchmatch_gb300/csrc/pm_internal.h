@@ -1,0 +1,120 @@
+// Internal types and helpers shared by the host-side translation units of the
+// densifier (pm_api.cu, pm_batch.cu): the opaque C ABI objects and the few
+// request helpers the batched executor reuses.  Not part of the public ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "pm_gb300.h"
+#include "pm_types.h"
+
+#define PM_INTERNAL __attribute__((visibility("hidden")))
+
+// Bearing tables of one image size (device).
+struct Trig {
+    int W = 0, H = 0;
+    float2 *row = nullptr, *col = nullptr;
+};
+
+
+struct pm_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    size_t budget = 0, used = 0;
+    std::string err;
+    uint64_t launches = 0;
+    std::vector<Trig> trig;
+    pm_request *cached = nullptr;
+    void *scratch = nullptr;
+    size_t scratch_bytes = 0;
+};
+
+struct pm_request {
+    pm_ctx *ctx = nullptr;
+    int W = 0, H = 0, S = 0;
+    pm_params prm{};
+    size_t bytes = 0;
+    void *block = nullptr;  // one device allocation holding everything below
+    float *ref = nullptr;
+    uint8_t *raw = nullptr;
+    void *quad[PM_MAX_SOURCES] = {};     // quad-packed footprints, or pitched images for textures
+    cudaTextureObject_t tex[PM_MAX_SOURCES] = {};
+    int tex_format = -1;                 // image format the texture objects were made for (-1: none)
+    size_t tex_pitch = 0;
+    uint8_t *mask = nullptr;
+    bool has_mask = false;
+    float4 *plane = nullptr;
+    float *score = nullptr;
+    int8_t *best = nullptr;
+    float *d0 = nullptr, *s0 = nullptr, *m1 = nullptr, *fdepth = nullptr, *fscore = nullptr;
+    float *x_depth = nullptr, *x_score = nullptr, *x_plane3 = nullptr, *x_normal3 = nullptr;
+    int32_t *x_best = nullptr;
+    float4 *seed = nullptr;              // seeding candidates from a prior result
+    unsigned long long *zbuf = nullptr;  // splat depth test of the prior warp
+    const pm_request *prior = nullptr;   // result reused as initialisation (may be null)
+    const pm_result *prior_res = nullptr;
+    int2 *lm = nullptr;                  // landmark seeds (pixel index, depth bits), device
+    int n_lm = 0, lm_cap = 0;
+    double R[PM_MAX_SOURCES + 1][9] = {}, t[PM_MAX_SOURCES + 1][3] = {};
+    bool have[PM_MAX_SOURCES + 1] = {};
+    Trig trig;
+    pm::SweepArgs args{};
+    cudaStream_t stream = nullptr;  // the request's own stream: requests overlap on the device
+    cudaEvent_t ready = nullptr;    // recorded on this stream for requests seeded from it
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    bool graph_dirty = true;
+    bool postprocessed = false;
+};
+
+// A retained keyframe result (plane state + filtered depth + pose): the
+// compact form in which results are kept for seeding later keyframes.
+struct pm_result {
+    pm_ctx *ctx = nullptr;
+    int W = 0, H = 0;
+    size_t bytes = 0;
+    void *block = nullptr;
+    float4 *plane = nullptr;
+    float *fdepth = nullptr;
+    double R[9] = {}, t[3] = {};
+    Trig trig;
+    cudaEvent_t ready = nullptr;  // recorded after the snapshot copies
+    bool valid = false;
+};
+
+namespace pmi {
+
+// Record the message of a failure on the context and return its status code.
+inline int fail(pm_ctx *ctx, int code, const char *fmt, ...) {
+    if (ctx) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        ctx->err = buf;
+    }
+    return code;
+}
+
+inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Kernel arguments of a request from its views, poses and parameters.
+PM_INTERNAL void fill_args(pm_request *r);
+// PM_EINVAL unless every view of the request has been set.
+PM_INTERNAL int check_views(pm_request *r);
+// Enqueue the post-filter of a request on `st` (its own stream when null).
+PM_INTERNAL int enqueue_post(pm_request *r, cudaStream_t st = nullptr);
+
+}  // namespace pmi
+
+#define PM_CUDA(ctx, call)                                                                                   \
+    do {                                                                                                     \
+        cudaError_t e_ = (call);                                                                             \
+        if (e_ != cudaSuccess) return pmi::fail((ctx), PM_ECUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)

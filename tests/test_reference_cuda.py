@@ -75,7 +75,7 @@ def test_converged_depth_agrees_with_reference_gpu_path(rk, ctx):
 
     def agree(a, b):
         both = (a > 0) & (b > 0)
-        return (np.abs(a - b) / b < 0.01)[both].mean(), both.mean()
+        return (np.abs(a[both] - b[both]) / b[both] < 0.01).mean(), both.mean()
 
     rr, rr_cov = agree(ref_f[1], ref_f[0])
     orf, or_cov = agree(ours, ref_f[0])
