@@ -68,9 +68,9 @@ __global__ void __launch_bounds__(kThreads, 2) batch_mixed_kernel(const __grid_c
 template <>
 cudaError_t launch_batch_mixed<PM_MIXED_KIND>(bool plain, int blocks, cudaStream_t st, const BatchArgs &b) {
     if (plain)
-        batch_mixed_kernel<true><<<blocks, kThreads, kTileSmemBytes, st>>>(b);
+        batch_mixed_kernel<true><<<blocks, kThreads, tile_kernel_smem_max(), st>>>(b);
     else
-        batch_mixed_kernel<false><<<blocks, kThreads, kTileSmemBytes, st>>>(b);
+        batch_mixed_kernel<false><<<blocks, kThreads, tile_kernel_smem_max(), st>>>(b);
     return cudaGetLastError();
 }
 
@@ -78,9 +78,9 @@ template <>
 int batch_mixed_blocks_per_sm<PM_MIXED_KIND>(bool plain) {
     int n = 0;
     if (plain)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_mixed_kernel<true>, kThreads, kTileSmemBytes);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_mixed_kernel<true>, kThreads, tile_kernel_smem_max());
     else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_mixed_kernel<false>, kThreads, kTileSmemBytes);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_mixed_kernel<false>, kThreads, tile_kernel_smem_max());
     return n;
 }
 

@@ -13,19 +13,22 @@ namespace {
 template <class Img>
 cudaError_t tile_launch(dim3 grid, cudaStream_t st, const SweepArgs &a) {
     if (a.propagation == PM_PROPAGATION_PLAIN)
-        tile_kernel<PM_INST_S, Img, true><<<grid, kThreads, kTileSmemBytes, st>>>(a);
+        tile_kernel<PM_INST_S, Img, true><<<grid, kThreads, tile_kernel_smem<PM_INST_S>(), st>>>(a);
     else
-        tile_kernel<PM_INST_S, Img, false><<<grid, kThreads, kTileSmemBytes, st>>>(a);
+        tile_kernel<PM_INST_S, Img, false><<<grid, kThreads, tile_kernel_smem<PM_INST_S>(), st>>>(a);
     return cudaGetLastError();
 }
 
 template <class Img>
 cudaError_t tile_smem_attr() {
-    cudaError_t e = cudaFuncSetAttribute(tile_kernel<PM_INST_S, Img, false>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmemBytes);
-    if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(tile_kernel<PM_INST_S, Img, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)kTileSmemBytes);
+    constexpr int dyn = (int)tile_kernel_smem<PM_INST_S>();
+    constexpr int blocks = tile_min_blocks<PM_INST_S>();
+    cudaError_t e = cudaFuncSetAttribute(tile_kernel<PM_INST_S, Img, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
+    e = e ? e : cudaFuncSetAttribute(tile_kernel<PM_INST_S, Img, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
+    e = e ? e : prefer_l1(tile_kernel<PM_INST_S, Img, false>, dyn, blocks);
+    e = e ? e : prefer_l1(tile_kernel<PM_INST_S, Img, true>, dyn, blocks);
+    e = e ? e : prefer_l1(batch_kernel<PM_INST_S, Img, false>, dyn, blocks);
+    return e ? e : prefer_l1(batch_kernel<PM_INST_S, Img, true>, dyn, blocks);
 }
 template <class Img>
 cudaError_t hyp_launch(int n, cudaStream_t st, const HypArgs &a) {
@@ -36,9 +39,9 @@ cudaError_t hyp_launch(int n, cudaStream_t st, const HypArgs &a) {
 template <class Img>
 cudaError_t batch_launch_img(bool plain, int blocks, cudaStream_t st, const BatchArgs &b) {
     if (plain)
-        batch_kernel<PM_INST_S, Img, true><<<blocks, kThreads, kTileSmemBytes, st>>>(b);
+        batch_kernel<PM_INST_S, Img, true><<<blocks, kThreads, tile_kernel_smem<PM_INST_S>(), st>>>(b);
     else
-        batch_kernel<PM_INST_S, Img, false><<<blocks, kThreads, kTileSmemBytes, st>>>(b);
+        batch_kernel<PM_INST_S, Img, false><<<blocks, kThreads, tile_kernel_smem<PM_INST_S>(), st>>>(b);
     return cudaGetLastError();
 }
 
@@ -46,10 +49,10 @@ template <class Img>
 int batch_occ(bool plain) {
     int n = 0;
     if (plain)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<PM_INST_S, Img, true>, kThreads, kTileSmemBytes);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<PM_INST_S, Img, true>, kThreads, tile_kernel_smem<PM_INST_S>());
     else
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<PM_INST_S, Img, false>, kThreads,
-                                                      kTileSmemBytes);
+                                                      tile_kernel_smem<PM_INST_S>());
     return n;
 }
 

@@ -25,11 +25,15 @@ constexpr int kTileRows = kTileH + 2 * kHaloMax;  // 18
 constexpr int kTileCols = (kTileW + 2 * kHaloMax) / 2;  // 37 same-colour entries per row
 constexpr int kMaxTaps = (kHaloMax + 1) * (kHaloMax + 1);
 
+constexpr int kTilePos = kTileRows * kTileCols;
+
 // Stage the same-colour (bearing, intensity) tile.  Entry (tr, cc) holds image
-// pixel (R, C) = (i0 - 5 + tr, x0 - 5 + 2 cc + ((R + colour + 1) & 1)).
+// pixel (R, C) = (i0 - 5 + tr, x0 - 5 + 2 cc + ((R + colour + 1) & 1)); the
+// bearing is (cos lat sin lon, -sin lat, cos lat cos lon).  Entries off the
+// image are 0.
 __device__ __forceinline__ void load_tile(float4 *tile, const float2 *row_trig, const float2 *col_trig,
                                           const float *ref, int W, int H, int i0, int x0, int colour) {
-    for (int e = threadIdx.x; e < kTileRows * kTileCols; e += blockDim.x) {
+    for (int e = threadIdx.x; e < kTilePos; e += blockDim.x) {
         const int tr = e / kTileCols, cc = e - tr * kTileCols;
         const int R = i0 - kHaloMax + tr;
         const int C = x0 - kHaloMax + 2 * cc + ((R + colour + 1) & 1);
@@ -43,22 +47,95 @@ __device__ __forceinline__ void load_tile(float4 *tile, const float2 *row_trig, 
 }
 
 // While a hypothesis is scored, the rest of a pixel visit's state (current
-// and candidate planes, score, depths, reference moments, loop counters) is
-// parked in shared memory, one 4-byte slot per value and thread, so that the
-// scoring loop keeps its S accumulation chains in registers without spilling.
-constexpr int kParkSlots = 24;
+// and candidate planes, score, depths, reference moments, packed counters
+// and coordinates) is parked in shared memory, one 4-byte slot per value and
+// thread, so that the scoring loop keeps its S accumulation chains in
+// registers without spilling.  The centre bearing is re-read from the tile.
+constexpr int kParkSlots = 17;
 
-// Dynamic shared memory of tile_kernel: the staged tile and the parked state;
-// the rest of the SM's unified L1/shared storage stays L1 for the samples.
-constexpr size_t kTileSmemBytes = sizeof(float4) * kTileRows * kTileCols + sizeof(float) * kParkSlots * kThreads;
+// Dynamic shared memory of tile_kernel: the staged tile, the parked state
+// and the warp factors (per source: A of both column parities, B of both
+// signs); the rest of the SM's unified L1/shared storage stays L1 for the
+// texture samples, whose hit rate sets the kernel's speed: the total per SM
+// is kept under the 100 KB carveout where the sources allow.
+constexpr int kFactorA = 2 * kTileCols;  // (column parity, same-colour column)
+constexpr int kFactorB = 2 * kTileRows;  // (sign, row)
+// Byte offsets: tile, parked state, factors.
+constexpr size_t kSmemPark = sizeof(float4) * kTilePos;
+constexpr size_t kSmemFactors = kSmemPark + sizeof(float) * kParkSlots * kThreads;
+constexpr size_t kTileSmemBytes = kSmemFactors;
+template <int S>
+__host__ __device__ constexpr size_t tile_kernel_smem() {
+    return kSmemFactors + (factored_warp<S>() ? sizeof(float4) * S * (kFactorA + kFactorB) : 0);
+}
+// Largest of the above over the source counts (the mixed batch kernel).
+__host__ __device__ constexpr size_t tile_kernel_smem_max() {
+    return tile_kernel_smem<PM_MAX_SOURCES>() > tile_kernel_smem<PM_FACTOR_MAX_SOURCES>()
+               ? tile_kernel_smem<PM_MAX_SOURCES>()
+               : tile_kernel_smem<PM_FACTOR_MAX_SOURCES>();
+}
+
+// Ask for the smallest shared-memory carveout that holds `blocks` CTAs of
+// `kernel` with `dyn` bytes of dynamic shared memory, leaving the rest of the
+// SM's unified storage to L1, where the texture samples hit (the driver's
+// default keeps a larger carveout).  The driver rounds the percentage up to
+// a supported size.
+template <class K>
+cudaError_t prefer_l1(K kernel, int dyn, int blocks) {
+    int dev = 0, per_sm = 0, reserved = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    e = e ? e : cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    e = e ? e : cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+    cudaFuncAttributes fa{};
+    e = e ? e : cudaFuncGetAttributes(&fa, kernel);
+    if (e != cudaSuccess || per_sm <= 0) return e;
+    const long long need = (long long)blocks * ((long long)dyn + (long long)fa.sharedSizeBytes + reserved);
+    const int pct = (int)((need * 100 + per_sm - 1) / per_sm);
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, pct < 100 ? pct : 100);
+}
+
+// Stage the warp factors of the tile: A(r, parity, cc) for image column
+// x0 - 5 + 2 cc + parity and B(r, sign, tr) for image row i0 - 5 + tr, the
+// latter as (sign B, sign cos lat) so that a tap reads sign(s) M_r b as
+// fma(B.w, A, B) with B picked by the sign of s.  Entries off the image are 0.
+template <int S, class Acc, class A>
+__device__ __forceinline__ void stage_factors(float4 *fac, const A &a, int i0, int x0) {
+    float4 *fa = fac, *fb = fac + S * kFactorA;
+    for (int e = threadIdx.x; e < S * (kFactorA + kFactorB); e += blockDim.x) {
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (e < S * kFactorA) {
+            const int r = e / kFactorA, q = e - r * kFactorA;
+            const int pa = q / kTileCols, cc = q - pa * kTileCols;
+            const int C = x0 - kHaloMax + 2 * cc + pa;
+            if (C >= 0 && C < a.W) {
+                const float2 ct = a.col_trig[C];
+                const float3 f = col_factor(Acc::row(a.P.G[r][0]), Acc::row(a.P.G[r][1]), Acc::row(a.P.G[r][2]), ct.x,
+                                            ct.y);
+                v = make_float4(f.x, f.y, f.z, 0.0f);
+            }
+            fa[e] = v;
+        } else {
+            const int eb = e - S * kFactorA;
+            const int r = eb / kFactorB, q = eb - r * kFactorB;
+            const int neg = q / kTileRows, tr = q - neg * kTileRows;
+            const int R = i0 - kHaloMax + tr;
+            if (R >= 0 && R < a.H) {
+                const float2 rt = a.row_trig[R];
+                const float3 f = row_factor(Acc::row(a.P.G[r][0]), Acc::row(a.P.G[r][1]), Acc::row(a.P.G[r][2]), rt.y);
+                const uint32_t sg = neg ? 0x80000000u : 0u;
+                v = make_float4(flip_sign(f.x, sg), flip_sign(f.y, sg), flip_sign(f.z, sg), flip_sign(rt.x, sg));
+            }
+            fb[eb] = v;
+        }
+    }
+}
 
 // Per-thread slots of the parked state.  The accesses are volatile so that
 // the compiler does not keep the values in registers across the scoring loop.
 struct Park {
     unsigned base;
-    __device__ __forceinline__ explicit Park(const float4 *tile)
-        : base((unsigned)__cvta_generic_to_shared(reinterpret_cast<const float *>(tile + kTileRows * kTileCols) +
-                                                  threadIdx.x)) {}
+    __device__ __forceinline__ explicit Park(const unsigned char *smem)
+        : base((unsigned)__cvta_generic_to_shared(reinterpret_cast<const float *>(smem + kSmemPark) + threadIdx.x)) {}
     __device__ __forceinline__ void put(int k, float v) const {
         asm volatile("st.shared.f32 [%0], %1;" ::"r"(base + 4u * kThreads * k), "f"(v) : "memory");
     }
@@ -113,7 +190,10 @@ template <int S, class Img, bool Plain, class Acc, class A>
 __device__ __forceinline__ void tile_body(const A &a, int bx, int by, float4 *tile) {
     const int tid = threadIdx.x, lane = tid & 31, ty = tid >> 5;
     const int x0 = bx * kTileW, i0 = by * kTileH;
+    unsigned char *const smem = reinterpret_cast<unsigned char *>(tile);
+    float4 *const fac = reinterpret_cast<float4 *>(smem + kSmemFactors);
     load_tile(tile, a.row_trig, a.col_trig, a.ref, a.W, a.H, i0, x0, a.colour);
+    if constexpr (factored_warp<S>()) stage_factors<S, Acc>(fac, a, i0, x0);
     __syncthreads();
 
     const int W = a.W, H = a.H, ph = a.patch_half;
@@ -122,12 +202,16 @@ __device__ __forceinline__ void tile_body(const A &a, int bx, int by, float4 *ti
     int j = x0 + 2 * lane + p;
     if (i < ph + 1 || i > H - ph - 1 || j < ph + 1 || j > W - ph - 1) return;  // PatchMatchCuda.cu:283
 
-    const float4 ctr = tile[(ty + kHaloMax) * kTileCols + ((2 * lane + p + kHaloMax) >> 1)];
+    const int ctr_e = (ty + kHaloMax) * kTileCols + ((2 * lane + p + kHaloMax) >> 1);
+    const float4 ctr = tile[ctr_e];
     float bxc = ctr.x, byc = ctr.y, bzc = ctr.z;
     const float Ic = ctr.w;
     const int nt = ph + 1;
     const int cbase = lane + ((kHaloMax - ph) >> 1);
     const int rbase = ty + kHaloMax - ph;
+    // column parity of the staged entries on this pixel's tap rows
+    // (rows rbase + 2 m1 of the tile: image rows i0 - 5 + rbase + 2 m1)
+    const int pa = (i0 + rbase + a.colour) & 1;
 
     // hypothesis-independent moments of the reference window; the bilateral
     // weights are recomputed per tap in the hypothesis loop (one MUFU.EX2 per
@@ -137,8 +221,7 @@ __device__ __forceinline__ void tile_body(const A &a, int bx, int by, float4 *ti
         const int k1 = 2 * m1 - ph;
         for (int m2 = 0; m2 < nt; ++m2) {
             const int k2 = 2 * m2 - ph;
-            const float4 e = tile[(rbase + 2 * m1) * kTileCols + cbase + m2];
-            const float xs = e.w - Ic;
+            const float xs = tile[(rbase + 2 * m1) * kTileCols + cbase + m2].w - Ic;
             const float w = bilateral_weight(xs, a.ncf, (float)(k1 * k1 + k2 * k2) * a.ndf);
             sw += w;
             swx = fmaf(w, xs, swx);
@@ -245,16 +328,18 @@ __device__ __forceinline__ void tile_body(const A &a, int bx, int by, float4 *ti
         }
         if (!found) break;
 
-        const Park park(tile);
-        park.save(hx, hy, hz, cx, cy, cz, score, current_depth, depth_hyp, f, sw, swx, swxx, bxc, byc, bzc, curr_depth,
-                  cand_w, best, h, kr, moved, i, j);
+        const Park park(smem);
+        // h < 16, kr < 8, i < 2^15, j < 2^15 (image sizes are validated)
+        park.save(hx, hy, hz, cx, cy, cz, score, current_depth, depth_hyp, f, sw, swx, swxx, curr_depth, cand_w,
+                  h | (kr << 4) | ((int)moved << 7) | (best << 8), i | (j << 16));
 
         // ---- cost of hypothesis (px, py, pz) ----
         TapAccum<S, Img, Acc> acc;
         acc.zero();
 #pragma unroll 1
         for (int m1 = 0; m1 < nt; ++m1) {
-            const float4 *trow = tile + (rbase + 2 * m1) * kTileCols + cbase;
+            const int tr = rbase + 2 * m1;
+            const float4 *trow = tile + tr * kTileCols + cbase;
             const int k1 = 2 * m1 - ph;
             const float dk1 = (float)(k1 * k1) * a.ndf;
 #pragma unroll 1
@@ -263,12 +348,37 @@ __device__ __forceinline__ void tile_body(const A &a, int bx, int by, float4 *ti
                 const int k2 = 2 * m2 - ph;
                 const float xs = e.w - Ic;
                 const float w = bilateral_weight(xs, Acc::val(a.ncf), fmaf((float)(k2 * k2), Acc::val(a.ndf), dk1));
-                acc.add(a.P, a.src, Acc::val(a.Wf), Acc::val(a.Hf), halfW, halfH, shift, px, py, pz, e.x, e.y, e.z, w,
-                        xs);
+                if constexpr (factored_warp<S>()) {
+                    const float s = fmaf(px, e.x, fmaf(py, e.y, pz * e.z));
+                    const float4 *fa = fac + pa * kTileCols + cbase + m2;
+                    const float4 *fb = fac + S * kFactorA + (s < 0.0f ? kTileRows : 0) + tr;
+                    acc.add_rot(a.P, a.src, Acc::val(a.Wf), Acc::val(a.Hf), halfW, halfH, shift, fabsf(s),
+                                [&](int r) {
+                                    const float4 A = fa[r * kFactorA], B = fb[r * kFactorB];
+                                    return make_float3(fmaf(B.w, A.x, B.x), fmaf(B.w, A.y, B.y), fmaf(B.w, A.z, B.z));
+                                },
+                                w, xs);
+                } else {
+                    acc.add_bearing(a.P, a.src, Acc::val(a.Wf), Acc::val(a.Hf), halfW, halfH, shift, px, py, pz, e.x,
+                                    e.y, e.z, w, xs);
+                }
             }
         }
-        park.load(hx, hy, hz, cx, cy, cz, score, current_depth, depth_hyp, f, sw, swx, swxx, bxc, byc, bzc, curr_depth,
-                  cand_w, best, h, kr, moved, i, j);
+        {
+            int st, ij;
+            park.load(hx, hy, hz, cx, cy, cz, score, current_depth, depth_hyp, f, sw, swx, swxx, curr_depth, cand_w, st,
+                      ij);
+            h = st & 15;
+            kr = (st >> 4) & 7;
+            moved = (st >> 7) & 1;
+            best = st >> 8;
+            i = ij & 0xffff;
+            j = ij >> 16;
+            const float4 c = tile[ctr_e];
+            bxc = c.x;
+            byc = c.y;
+            bzc = c.z;
+        }
         idx = (size_t)i * W + j;
         float sep[S], cum[S];
         source_nccs(acc, sw, swx, swxx, a.combine, sep, cum);
@@ -377,8 +487,7 @@ __global__ void __launch_bounds__(256) hyp_kernel(const __grid_constant__ HypArg
             sw += w;
             swx = fmaf(w, xs, swx);
             swxx = fmaf(w * xs, xs, swxx);
-            acc.add(a.P, a.src, a.Wf, a.Hf, halfW, halfH, shift, px, py, pz, rt.x * ct.x, -rt.y,
-                    rt.x * ct.y, w, xs);
+            acc.add_trig(a.P, a.src, a.Wf, a.Hf, halfW, halfH, shift, px, py, pz, rt, ct, w, xs);
         }
     }
     float sep[S], cum[S];
