@@ -354,8 +354,9 @@ __device__ __forceinline__ void tile_body(const A &a, int bx, int by, float4 *ti
                     const float4 *fb = fac + S * kFactorA + (s < 0.0f ? kTileRows : 0) + tr;
                     acc.add_rot(a.P, a.src, Acc::val(a.Wf), Acc::val(a.Hf), halfW, halfH, shift, fabsf(s),
                                 [&](int r) {
-                                    const float4 A = fa[r * kFactorA], B = fb[r * kFactorB];
-                                    return make_float3(fmaf(B.w, A.x, B.x), fmaf(B.w, A.y, B.y), fmaf(B.w, A.z, B.z));
+                                    const float4 ca = fa[r * kFactorA], rb = fb[r * kFactorB];
+                                    return make_float3(fmaf(rb.w, ca.x, rb.x), fmaf(rb.w, ca.y, rb.y),
+                                                       fmaf(rb.w, ca.z, rb.z));
                                 },
                                 w, xs);
                 } else {
