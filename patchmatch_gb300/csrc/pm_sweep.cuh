@@ -7,10 +7,12 @@
 // pixel).  All window taps of a pixel of colour c are themselves pixels of
 // colour c, so the CTA stages only those: an 18 x 37 shared-memory tile of
 // (bearing, intensity) float4 including the 5-pixel halo, indexed so that the
-// 32 lanes of a warp read 32 consecutive entries.  Per-pixel bilateral weights
-// and the hypothesis-independent reference moments are computed once per
-// visit; the inner loop then evaluates each hypothesis over the 36 taps and S
-// sources with S independent accumulation chains.
+// 32 lanes of a warp read 32 consecutive entries.  The hypothesis-independent
+// reference moments are computed once per visit; the inner loop then
+// evaluates each hypothesis over the 36 taps and S sources with S independent
+// accumulation chains (recomputing each tap's bilateral weight, one MUFU.EX2
+// shared by the sources).  From 8 sources the CTA also stages the row and
+// column factors of the warp (see stage_factors).
 #pragma once
 
 #include "pm_device.cuh"
