@@ -76,6 +76,9 @@ __host__ __device__ constexpr size_t tile_kernel_smem_max() {
                ? tile_kernel_smem<PM_MAX_SOURCES>()
                : tile_kernel_smem<PM_FACTOR_MAX_SOURCES>();
 }
+// The mixed batch kernel launches without raising its dynamic shared-memory
+// limit, so every layout stays within the default 48 KB.
+static_assert(tile_kernel_smem_max() <= 48 * 1024, "tile layout exceeds the default dynamic shared memory");
 
 // Ask for the smallest shared-memory carveout that holds `blocks` CTAs of
 // `kernel` with `dyn` bytes of dynamic shared memory, leaving the rest of the
