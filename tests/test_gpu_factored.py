@@ -27,14 +27,16 @@ def _request(ctx, req, **kw):
 
 
 @pytest.mark.parametrize("sampler", [native.SAMPLER_EXACT, native.SAMPLER_TEXTURE])
-@pytest.mark.parametrize("n_src", [4, 8, 10])
-def test_tile_scores_equal_fixed_hypothesis_scores(ctx, n_src, sampler):
-    req = scene.make_request(scene.ROOM_OBJECTS, W, H, n_src, seed=60 + n_src, bmin=0.1, bmax=0.6)
+@pytest.mark.parametrize("n_src,w,h", [(4, W, H), (8, W, H), (10, W, H), (9, 131, 67)])
+def test_tile_scores_equal_fixed_hypothesis_scores(ctx, n_src, w, h, sampler):
+    """131x67 leaves the last tile column and row partly off the image, where
+    the staged factors of off-image columns and rows are 0."""
+    req = scene.make_request(scene.ROOM_OBJECTS, w, h, n_src, seed=60 + n_src, bmin=0.1, bmax=0.6)
     r = _request(ctx, req, sampler=sampler, iterations=0, postprocess=0)
     r.init()
     g = r.read(raw=True)
     ph = 5
-    ii, jj = np.mgrid[ph + 1:H - ph, ph + 1:W - ph]
+    ii, jj = np.mgrid[ph + 1:h - ph, ph + 1:w - ph]
     ij = np.stack([ii.ravel(), jj.ravel()], 1).astype(np.int32)
     planes = np.ascontiguousarray(g["plane"][ii.ravel(), jj.ravel(), :3], np.float32)
     s, best = r.score_hypotheses(ij, planes)
