@@ -334,7 +334,10 @@ int pm_server_create(pm_ctx *ctx, const pm_server_config *cfg, pm_server **out);
 int pm_server_submit(pm_server *srv, int width, int height, const pm_view *keyframe, uint64_t *ticket);
 /* Blocks until the ticket's keyframe is done (timeout_ms < 0: no limit;
  * PM_ETIMEOUT otherwise), then fills out->depth / out->score (host, may be
- * NULL) and info.  Returns the keyframe's status. */
+ * NULL) and info.  Returns the keyframe's status.  Each ticket is collected
+ * once: PM_EINVAL for a ticket this server did not issue or that was already
+ * collected (also when another thread collects it while this one waits).
+ * All waits must have returned before pm_server_destroy. */
 int pm_server_wait(pm_server *srv, uint64_t ticket, int timeout_ms, pm_maps *out, pm_served_info *info);
 /* Finishes all submitted keyframes, then releases everything. */
 int pm_server_destroy(pm_server *srv);

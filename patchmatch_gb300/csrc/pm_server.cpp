@@ -18,6 +18,7 @@
 #include <mutex>
 #include <thread>
 #include <unordered_map>
+#include <unordered_set>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -204,6 +205,7 @@ struct pm_server {
     // never depends on timing.  Pruned to what a later keyframe can still use.
     std::map<uint64_t, std::shared_ptr<ResHolder>> priors;
     std::unordered_map<uint64_t, Result> done;
+    std::unordered_set<uint64_t> outstanding;  // issued and not yet collected by pm_server_wait
 };
 
 namespace {
@@ -629,6 +631,7 @@ int pm_server_submit(pm_server *s, int W, int H, const pm_view *view, uint64_t *
     if (s->stop) return PM_ECANCELLED;
     sub.ticket = s->next_ticket++;
     *ticket = sub.ticket;
+    s->outstanding.insert(sub.ticket);
     s->pending.push_back(std::move(sub));
     s->cv_work.notify_one();
     return PM_OK;
@@ -637,14 +640,19 @@ int pm_server_submit(pm_server *s, int W, int H, const pm_view *view, uint64_t *
 int pm_server_wait(pm_server *s, uint64_t ticket, int timeout_ms, pm_maps *out, pm_served_info *info) {
     if (!s) return PM_EINVAL;
     std::unique_lock<std::mutex> lk(s->mu);
-    const auto pred = [&] { return s->done.count(ticket) > 0; };
+    if (!s->outstanding.count(ticket)) return PM_EINVAL;  // never issued, or already collected
+    // also wakes when another thread collects the ticket first
+    const auto pred = [&] { return s->done.count(ticket) > 0 || !s->outstanding.count(ticket); };
     if (timeout_ms < 0)
         s->cv_done.wait(lk, pred);
     else if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), pred))
         return PM_ETIMEOUT;
+    if (!s->done.count(ticket)) return PM_EINVAL;
     Result r = std::move(s->done[ticket]);
     s->done.erase(ticket);
+    s->outstanding.erase(ticket);
     lk.unlock();
+    s->cv_done.notify_all();
     if (info) *info = r.info;
     if (out && r.status == PM_OK) {
         if (out->depth) std::memcpy(out->depth, r.depth.data(), r.depth.size() * 4);

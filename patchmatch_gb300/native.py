@@ -635,7 +635,7 @@ class Server:
 
     def wait(self, ticket: int, timeout_ms: int = -1, want_score: bool = False):
         """Returns (status, depth or None, score or None, info dict)."""
-        H, W = self.shape.pop(ticket)
+        H, W = self.shape[ticket]
         depth = np.zeros((H, W), np.float32)
         score = np.zeros((H, W), np.float32) if want_score else None
         m = Maps()
@@ -643,6 +643,8 @@ class Server:
         m.score = score.ctypes.data if want_score else None
         info = ServedInfo()
         rc = self._L.pm_server_wait(self.h, ticket, timeout_ms, C.byref(m), C.byref(info))
+        if rc != PM_ETIMEOUT:  # collected (or rejected): the ticket is gone
+            self.shape.pop(ticket, None)
         d = {k: getattr(info, k) for k, _ in ServedInfo._fields_}
         ok = rc == PM_OK
         return rc, (depth if ok else None), (score if ok else None), d

@@ -171,3 +171,17 @@ def test_mixed_sizes_alone_and_in_the_mix(ctx):
             n_same = sum(1 for j in range(k) if views[j].gray_u8.shape == v.gray_u8.shape)
             assert a[3]["n_sources"] <= n_same
     assert dense >= 6
+
+
+def test_tickets_are_collected_once(ctx, stream_views):
+    """pm_server_wait rejects a ticket the server never issued and one that
+    was already collected (PM_EINVAL) instead of blocking forever."""
+    srv = native.Server(ctx, _cfg(1))
+    L = srv._L
+    assert L.pm_server_wait(srv.h, 12345, -1, None, None) == native.PM_EINVAL
+    v = stream_views[0]
+    tk = srv.submit(v.gray_u8, v.R, v.t)
+    st, _, _, _ = srv.wait(tk)  # the first keyframe has no neighbours yet
+    assert st == native.PM_ENOTREADY
+    assert L.pm_server_wait(srv.h, tk, -1, None, None) == native.PM_EINVAL
+    srv.close()
