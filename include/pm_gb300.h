@@ -385,7 +385,9 @@ int pm_fuse_noalloc(int width, int height, int n_views, float *const *depths, co
  * pm_request_run bit for bit.  Requests keep their own buffers and streams:
  * set their views before pm_batch_run; read them afterwards with
  * pm_request_read (their streams wait for the batch).  Seeding (priors,
- * landmarks) is not batched (PM_EINVAL).  pm_batch_tune runs the batch once
+ * landmarks) is not batched (PM_EINVAL).  A request in a batch cannot be
+ * destroyed (pm_request_destroy returns PM_EINVAL) until pm_batch_clear or
+ * pm_batch_destroy releases it.  pm_batch_tune runs the batch once
  * per executor candidate, keeps the fastest and reports the timings.
  * No counterpart in the reference (one keyframe at a time,
  * depthmap_computation_module.cc:205-472). */

@@ -753,6 +753,8 @@ int pm_request_create(pm_ctx *ctx, int W, int H, int S, const pm_params *params,
 int pm_request_destroy(pm_request *r) {
     if (!r) return PM_EINVAL;
     pm_ctx *ctx = r->ctx;
+    if (r->batch_refs > 0)
+        return fail(ctx, PM_EINVAL, "request is in %d batch(es): clear or destroy them first", r->batch_refs);
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(r->stream);
     if (r->gexec) cudaGraphExecDestroy(r->gexec);

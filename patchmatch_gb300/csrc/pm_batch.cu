@@ -254,6 +254,7 @@ int pm_batch_add(pm_batch *b, pm_request *r) {
         return fail(b->ctx, PM_ECUDA, "event creation failed");
     }
     b->req_events.push_back(e);
+    ++r->batch_refs;
     b->dirty = true;
     return PM_OK;
 }
@@ -263,6 +264,7 @@ int pm_batch_clear(pm_batch *b) {
     cudaStreamSynchronize(b->stream);
     for (cudaEvent_t e : b->req_events) cudaEventDestroy(e);
     b->req_events.clear();
+    for (pm_request *r : b->reqs) --r->batch_refs;
     b->reqs.clear();
     b->dirty = true;
     return PM_OK;
@@ -409,6 +411,7 @@ int pm_batch_destroy(pm_batch *b) {
     if (b->graph) cudaGraphDestroy(b->graph);
     batch_free_groups(b);
     for (cudaEvent_t e : b->req_events) cudaEventDestroy(e);
+    for (pm_request *r : b->reqs) --r->batch_refs;
     for (int k = 0; k < pm_batch::kBranches; ++k) {
         if (b->branch[k]) cudaStreamDestroy(b->branch[k]);
         if (b->join[k]) cudaEventDestroy(b->join[k]);

@@ -37,6 +37,7 @@ struct pm_ctx {
 struct pm_request {
     pm_ctx *ctx = nullptr;
     int W = 0, H = 0, S = 0;
+    int batch_refs = 0;  // batches holding this request (it cannot be destroyed meanwhile)
     pm_params prm{};
     size_t bytes = 0;
     void *block = nullptr;  // one device allocation holding everything below

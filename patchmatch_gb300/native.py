@@ -427,7 +427,8 @@ class Request:
 
     def close(self):
         if getattr(self, "h", None):
-            self._L.pm_request_destroy(self.h)
+            # fails (and keeps the request) while a batch still holds it
+            self.ctx.check(self._L.pm_request_destroy(self.h))
             self.h = None
 
     def __del__(self):

@@ -85,3 +85,20 @@ def test_batch_rejects_seeded_requests(ctx, batch_requests):
     b.close()
     for r in rs:
         r.close()
+
+
+def test_request_in_a_batch_cannot_be_destroyed(ctx):
+    """pm_request_destroy refuses a request a batch still holds (the batch
+    would run on freed memory); clearing the batch releases it."""
+    req = scene.make_request(scene.ROOM, 128, 64, 2, seed=5)
+    r = ctx.request(128, 64, 2, native.default_params(iterations=2))
+    r.set_views([v.gray_u8 for v in req.views], req.R, req.t)
+    b = native.Batch(ctx, [r])
+    with pytest.raises(native.PmError) as e:
+        r.close()
+    assert e.value.status == native.PM_EINVAL
+    b.run()
+    b.synchronize()
+    b.clear()
+    r.close()
+    b.close()
