@@ -221,7 +221,9 @@ int pm_request_set_prior(pm_request *req, const pm_request *prior);
  * keyframes while the request itself is reused.  pm_result_snapshot enqueues
  * the copy on the request's stream (the request must have been
  * post-processed); pm_request_set_prior_result makes pm_request_run seed from
- * it once the copy has finished.  The result must stay alive until then. */
+ * it once the copy has finished.  A prior link (to a request or a result)
+ * lasts until it is replaced; destroying the prior waits for its dependents'
+ * in-flight work and unlinks them, so their next run starts unseeded. */
 size_t pm_result_bytes(int width, int height);
 int pm_result_create(pm_ctx *ctx, int width, int height, pm_result **out);
 int pm_result_snapshot(pm_result *res, pm_request *req);

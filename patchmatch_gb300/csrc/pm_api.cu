@@ -27,6 +27,8 @@ using pmi::align256;
 using pmi::fill_args;
 using pmi::check_views;
 using pmi::enqueue_post;
+using pmi::link_prior;
+using pmi::unlink_dependents;
 
 namespace {
 
@@ -154,6 +156,29 @@ int validate_size(pm_ctx *ctx, int W, int H, int S) {
 }
 
 }  // namespace
+
+void pmi::link_prior(pm_request *r, const pm_request *prior, const pm_result *res) {
+    const auto drop = [r](std::vector<pm_request *> &v) { v.erase(std::remove(v.begin(), v.end(), r), v.end()); };
+    if (r->prior) drop(r->prior->dependents);
+    if (r->prior_res) drop(r->prior_res->dependents);
+    r->prior = prior;
+    r->prior_res = res;
+    if (prior) prior->dependents.push_back(r);
+    if (res) res->dependents.push_back(r);
+    r->graph_dirty = true;
+}
+
+void pmi::unlink_dependents(std::vector<pm_request *> &deps, bool from_request) {
+    for (pm_request *d : deps) {
+        cudaStreamSynchronize(d->stream);
+        if (from_request)
+            d->prior = nullptr;
+        else
+            d->prior_res = nullptr;
+        d->graph_dirty = true;
+    }
+    deps.clear();
+}
 
 void pmi::fill_args(pm_request *r) {
     pm::SweepArgs &a = r->args;
@@ -756,6 +781,8 @@ int pm_request_destroy(pm_request *r) {
     if (r->batch_refs > 0)
         return fail(ctx, PM_EINVAL, "request is in %d batch(es): clear or destroy them first", r->batch_refs);
     cudaSetDevice(ctx->device);
+    unlink_dependents(r->dependents, true);
+    link_prior(r, nullptr, nullptr);
     cudaStreamSynchronize(r->stream);
     if (r->gexec) cudaGraphExecDestroy(r->gexec);
     if (r->graph) cudaGraphDestroy(r->graph);
@@ -884,18 +911,14 @@ int pm_request_set_prior(pm_request *r, const pm_request *prior) {
     if (!r) return PM_EINVAL;
     if (prior && prior->ctx != r->ctx) return fail(r->ctx, PM_EINVAL, "prior belongs to another context");
     if (prior == r) return fail(r->ctx, PM_EINVAL, "a request cannot seed itself");
-    r->prior = prior;
-    r->prior_res = nullptr;
-    r->graph_dirty = true;
+    link_prior(r, prior, nullptr);
     return PM_OK;
 }
 
 int pm_request_set_prior_result(pm_request *r, const pm_result *res) {
     if (!r) return PM_EINVAL;
     if (res && res->ctx != r->ctx) return fail(r->ctx, PM_EINVAL, "result belongs to another context");
-    r->prior_res = res;
-    r->prior = nullptr;
-    r->graph_dirty = true;
+    link_prior(r, nullptr, res);
     return PM_OK;
 }
 
@@ -955,6 +978,7 @@ int pm_result_snapshot(pm_result *res, pm_request *r) {
 int pm_result_destroy(pm_result *res) {
     if (!res) return PM_EINVAL;
     cudaSetDevice(res->ctx->device);
+    unlink_dependents(res->dependents, false);
     cudaEventSynchronize(res->ready);
     cudaEventDestroy(res->ready);
     cudaFree(res->block);

@@ -59,6 +59,8 @@ struct pm_request {
     unsigned long long *zbuf = nullptr;  // splat depth test of the prior warp
     const pm_request *prior = nullptr;   // result reused as initialisation (may be null)
     const pm_result *prior_res = nullptr;
+    // requests whose prior is this one: unlinked when it is destroyed
+    mutable std::vector<pm_request *> dependents;
     int2 *lm = nullptr;                  // landmark seeds (pixel index, depth bits), device
     int n_lm = 0, lm_cap = 0;
     double R[PM_MAX_SOURCES + 1][9] = {}, t[PM_MAX_SOURCES + 1][3] = {};
@@ -86,6 +88,8 @@ struct pm_result {
     Trig trig;
     cudaEvent_t ready = nullptr;  // recorded after the snapshot copies
     bool valid = false;
+    // requests whose prior is this result: unlinked when it is destroyed
+    mutable std::vector<pm_request *> dependents;
 };
 
 namespace pmi {
@@ -111,6 +115,12 @@ PM_INTERNAL void fill_args(pm_request *r);
 PM_INTERNAL int check_views(pm_request *r);
 // Enqueue the post-filter of a request on `st` (its own stream when null).
 PM_INTERNAL int enqueue_post(pm_request *r, cudaStream_t st = nullptr);
+// Replace the prior links of r (request or retained result, at most one set),
+// keeping the priors' dependent lists in step.
+PM_INTERNAL void link_prior(pm_request *r, const pm_request *prior, const pm_result *res);
+// Unlink every dependent of a prior that is being destroyed, after the
+// dependents' in-flight work (which may read the prior) has finished.
+PM_INTERNAL void unlink_dependents(std::vector<pm_request *> &deps, bool from_request);
 
 }  // namespace pmi
 

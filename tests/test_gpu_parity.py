@@ -502,3 +502,37 @@ def test_size_limits_are_rejected(ctx):
         with pytest.raises(native.PmError) as e:
             ctx.request(W, H, 2, native.default_params())
         assert e.value.status == native.PM_EINVAL, (W, H)
+
+
+def test_destroyed_prior_is_unlinked(ctx, room):
+    """Destroying a request's prior (a request or a retained result) unlinks
+    it: the next run starts unseeded and equals a never-seeded run bit for bit."""
+    def fresh():
+        return _req_on_gpu(ctx, room, iterations=2)
+
+    ref = fresh()
+    ref.run()
+    want = ref.read(raw=True)
+    for kind in ("request", "result"):
+        prior = fresh()
+        prior.run()
+        holder = prior
+        if kind == "result":
+            holder = native.Result(ctx, W1, H1)
+            holder.snapshot(prior)
+        r = fresh()
+        r.set_prior(holder)
+        r.run()
+        seeded = r.read(raw=True)
+        assert not np.array_equal(seeded["plane"], want["plane"])  # the prior was used
+        holder.close()
+        if kind == "result":
+            prior.close()
+        r.run()
+        got = r.read(raw=True)
+        for k in ("plane", "score", "depth"):
+            assert np.array_equal(got[k], want[k]), (kind, k)
+        if kind == "request":
+            prior.close()
+        r.close()
+    ref.close()
