@@ -149,10 +149,11 @@ void pm_params_default(pm_params *p);
  * retained results, batches) are used from one host thread at a time; a
  * pm_server works on its context from its own worker thread, so make no
  * other calls on that context while the server exists.  Several contexts
- * may run side by side.  A request added to a batch, and a request or
- * retained result set as a prior, must stay alive until the batch is cleared
- * or destroyed or the prior is replaced; destroy servers, batches, requests
- * and results before their context. */
+ * may run side by side.  A request held by a batch cannot be destroyed
+ * until the batch is cleared or destroyed; destroying a prior (request or
+ * retained result) unlinks the requests it seeds.  pm_destroy returns
+ * PM_EINVAL while requests, retained results or batches of the context are
+ * alive: destroy servers, batches, requests and results first. */
 int pm_create(int device, size_t hbm_budget_bytes, pm_ctx **out);
 int pm_destroy(pm_ctx *ctx);
 const char *pm_last_error(const pm_ctx *ctx);

@@ -643,6 +643,9 @@ int pm_create(int device, size_t hbm_budget_bytes, pm_ctx **out) {
 
 int pm_destroy(pm_ctx *ctx) {
     if (!ctx) return PM_EINVAL;
+    if (ctx->live > (ctx->cached ? 1 : 0))
+        return fail(ctx, PM_EINVAL, "%d request(s), result(s) or batch(es) of this context are still alive",
+                    ctx->live - (ctx->cached ? 1 : 0));
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     if (ctx->cached) pm_request_destroy(ctx->cached);
@@ -771,6 +774,7 @@ int pm_request_create(pm_ctx *ctx, int W, int H, int S, const pm_params *params,
     r->seed = (float4 *)take(N * 16);
     r->zbuf = (unsigned long long *)take(N * 8);
     ctx->used += bytes;
+    ++ctx->live;
     *out = r;
     return PM_OK;
 }
@@ -792,6 +796,7 @@ int pm_request_destroy(pm_request *r) {
     cudaStreamDestroy(r->stream);
     cudaFree(r->block);
     ctx->used -= r->bytes;
+    --ctx->live;
     if (ctx->cached == r) ctx->cached = nullptr;
     delete r;
     return PM_OK;
@@ -955,6 +960,7 @@ int pm_result_create(pm_ctx *ctx, int W, int H, pm_result **out) {
     r->plane = (float4 *)r->block;
     r->fdepth = (float *)((char *)r->block + align256((size_t)W * H * 16));
     ctx->used += bytes;
+    ++ctx->live;
     *out = r;
     return PM_OK;
 }
@@ -983,6 +989,7 @@ int pm_result_destroy(pm_result *res) {
     cudaEventDestroy(res->ready);
     cudaFree(res->block);
     res->ctx->used -= res->bytes;
+    --res->ctx->live;
     delete res;
     return PM_OK;
 }

@@ -226,6 +226,7 @@ int pm_batch_create(pm_ctx *ctx, pm_batch **out) {
     PM_CUDA(ctx, cudaSetDevice(ctx->device));
     pm_batch *b = new pm_batch();
     b->ctx = ctx;
+    ++ctx->live;
     bool ok = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) == cudaSuccess &&
               cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming) == cudaSuccess &&
               cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) == cudaSuccess;
@@ -419,6 +420,7 @@ int pm_batch_destroy(pm_batch *b) {
     if (b->fork) cudaEventDestroy(b->fork);
     if (b->done) cudaEventDestroy(b->done);
     if (b->stream) cudaStreamDestroy(b->stream);
+    --b->ctx->live;
     delete b;
     return PM_OK;
 }

@@ -32,6 +32,7 @@ struct pm_ctx {
     pm_request *cached = nullptr;
     void *scratch = nullptr;
     size_t scratch_bytes = 0;
+    int live = 0;  // requests, retained results and batches made from this context (cached included)
 };
 
 struct pm_request {

@@ -272,8 +272,9 @@ class Context:
         self.h = h.value
 
     def close(self):
-        if getattr(self, "h", None):
-            self._L.pm_destroy(self.h)
+        # pm_destroy refuses while requests, results or batches are alive; the
+        # handle is then kept (their finalisers still need the context)
+        if getattr(self, "h", None) and self._L.pm_destroy(self.h) == PM_OK:
             self.h = None
 
     def __del__(self):

@@ -536,3 +536,18 @@ def test_destroyed_prior_is_unlinked(ctx, room):
             prior.close()
         r.close()
     ref.close()
+
+
+def test_context_outlives_its_objects(built):
+    """pm_destroy refuses while a request, retained result or batch of the
+    context is alive (their destroy would touch the freed context)."""
+    c = native.Context(0)
+    L = c._L
+    r = c.request(64, 32, 2, native.default_params())
+    res = native.Result(c, 64, 32)
+    b = native.Batch(c)
+    for obj in (b, res, r):
+        assert L.pm_destroy(c.h) == native.PM_EINVAL
+        obj.close()
+    c.close()
+    assert c.h is None
