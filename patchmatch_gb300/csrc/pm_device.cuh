@@ -303,11 +303,13 @@ __device__ __forceinline__ float3 rotate(const float4 &g0, const float4 &g1, con
 // three FMAs and two shared-memory reads per source instead of nine FMAs.
 // Used from PM_FACTOR_MIN_SOURCES to PM_FACTOR_MAX_SOURCES sources: with
 // fewer sources the shared-memory reads cost as much as the FMAs they
-// replace (measured at 1920x960: 4-6 sources faster direct, 8 even, 10
-// sources 4 % faster factored).  The staged factors take 1760 bytes of shared
-// memory per source.
+// replace and the staged factors take L1 from the texture samples (measured,
+// 8 sweeps: 1920x960 u8 - 4-6 sources faster direct, 8 even, 10 sources 4 %
+// faster factored; 3840x1920 - 8 sources FP16 4 % faster direct, 9-10
+// sources 0-3 % faster factored).  The staged factors take 1760 bytes of
+// shared memory per source.
 #ifndef PM_FACTOR_MIN_SOURCES
-#define PM_FACTOR_MIN_SOURCES 8
+#define PM_FACTOR_MIN_SOURCES 9
 #endif
 #ifndef PM_FACTOR_MAX_SOURCES
 #define PM_FACTOR_MAX_SOURCES 10

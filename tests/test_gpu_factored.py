@@ -1,4 +1,4 @@
-"""The factored warp of the tile kernel (8 to 10 sources) and the direct
+"""The factored warp of the tile kernel (9 and 10 sources) and the direct
 rotation (fewer sources), through the C ABI.
 
 The tile kernel stages per-column and per-row factors of M_r b in shared
@@ -48,7 +48,7 @@ def test_tile_scores_equal_fixed_hypothesis_scores(ctx, n_src, w, h, sampler):
     assert (best == g["best_view"][ii.ravel(), jj.ravel()]).all()
 
 
-@pytest.mark.parametrize("n_src", [8, 10])
+@pytest.mark.parametrize("n_src", [9, 10])
 def test_factored_half_sweeps_match_oracle(ctx, n_src):
     """One red and one black half-sweep from an identical state with the
     factored warp: the chosen planes match the FP64 oracle's except where two
