@@ -11,7 +11,16 @@ namespace pm {
 
 namespace {
 template <class Img>
-cudaError_t tile_launch(dim3 grid, cudaStream_t st, const SweepArgs &a) {
+cudaError_t tile_launch(dim3 grid, cudaStream_t st, const SweepArgs &a, const BandArgs *band) {
+    if (band) {
+        if (a.propagation == PM_PROPAGATION_PLAIN)
+            tile_kernel_banded<PM_INST_S, Img, true><<<band->blocks, kThreads, tile_kernel_smem<PM_INST_S>(), st>>>(
+                a, *band);
+        else
+            tile_kernel_banded<PM_INST_S, Img, false><<<band->blocks, kThreads, tile_kernel_smem<PM_INST_S>(), st>>>(
+                a, *band);
+        return cudaGetLastError();
+    }
     if (a.propagation == PM_PROPAGATION_PLAIN)
         tile_kernel<PM_INST_S, Img, true><<<grid, kThreads, tile_kernel_smem<PM_INST_S>(), st>>>(a);
     else
@@ -28,7 +37,21 @@ cudaError_t tile_smem_attr() {
     e = e ? e : prefer_l1(tile_kernel<PM_INST_S, Img, false>, dyn, blocks);
     e = e ? e : prefer_l1(tile_kernel<PM_INST_S, Img, true>, dyn, blocks);
     e = e ? e : prefer_l1(batch_kernel<PM_INST_S, Img, false>, dyn, blocks);
-    return e ? e : prefer_l1(batch_kernel<PM_INST_S, Img, true>, dyn, blocks);
+    e = e ? e : prefer_l1(batch_kernel<PM_INST_S, Img, true>, dyn, blocks);
+    e = e ? e : cudaFuncSetAttribute(tile_kernel_banded<PM_INST_S, Img, false>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
+    e = e ? e : cudaFuncSetAttribute(tile_kernel_banded<PM_INST_S, Img, true>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
+    e = e ? e : prefer_l1(tile_kernel_banded<PM_INST_S, Img, false>, dyn, blocks);
+    return e ? e : prefer_l1(tile_kernel_banded<PM_INST_S, Img, true>, dyn, blocks);
+}
+
+template <class Img>
+int banded_occ() {
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, tile_kernel_banded<PM_INST_S, Img, false>, kThreads,
+                                                  tile_kernel_smem<PM_INST_S>());
+    return n;
 }
 template <class Img>
 cudaError_t hyp_launch(int n, cudaStream_t st, const HypArgs &a) {
@@ -72,12 +95,22 @@ cudaError_t configure_tile<PM_INST_S>() {
 
 // kind: kImageQuadU8, kImageQuadF16, kImageTexU8, kImageTexF16
 template <>
-cudaError_t launch_tile<PM_INST_S>(int kind, dim3 grid, cudaStream_t st, const SweepArgs &a) {
+cudaError_t launch_tile<PM_INST_S>(int kind, dim3 grid, cudaStream_t st, const SweepArgs &a, const BandArgs *band) {
     switch (kind) {
-        case kImageQuadF16: return tile_launch<QuadF16>(grid, st, a);
-        case kImageTexU8: return tile_launch<TexU8>(grid, st, a);
-        case kImageTexF16: return tile_launch<TexF16>(grid, st, a);
-        default: return tile_launch<QuadU8>(grid, st, a);
+        case kImageQuadF16: return tile_launch<QuadF16>(grid, st, a, band);
+        case kImageTexU8: return tile_launch<TexU8>(grid, st, a, band);
+        case kImageTexF16: return tile_launch<TexF16>(grid, st, a, band);
+        default: return tile_launch<QuadU8>(grid, st, a, band);
+    }
+}
+
+template <>
+int tile_blocks_per_sm<PM_INST_S>(int kind) {
+    switch (kind) {
+        case kImageQuadF16: return banded_occ<QuadF16>();
+        case kImageTexU8: return banded_occ<TexU8>();
+        case kImageTexF16: return banded_occ<TexF16>();
+        default: return banded_occ<QuadU8>();
     }
 }
 

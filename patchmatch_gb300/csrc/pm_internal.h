@@ -33,12 +33,15 @@ struct pm_ctx {
     void *scratch = nullptr;
     size_t scratch_bytes = 0;
     int live = 0;  // requests, retained results and batches made from this context (cached included)
+    int n_sm = 0;  // streaming multiprocessors: bands of the banded tile order
 };
 
 struct pm_request {
     pm_ctx *ctx = nullptr;
     int W = 0, H = 0, S = 0;
     int batch_refs = 0;  // batches holding this request (it cannot be destroyed meanwhile)
+    unsigned *band_ctr = nullptr;  // per-SM tile counters of the banded order (in the block)
+    int banded_blocks = 0;         // persistent grid of the banded order (0: one CTA per tile)
     pm_params prm{};
     size_t bytes = 0;
     void *block = nullptr;  // one device allocation holding everything below

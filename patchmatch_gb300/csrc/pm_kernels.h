@@ -25,8 +25,11 @@ inline int image_kind(int image_format, int sampler) {
 }
 
 // pm_inst.cu (one translation unit per source count S)
+// band: null for one CTA per tile over `grid`, else the banded persistent order
 template <int S>
-cudaError_t launch_tile(int kind, dim3 grid, cudaStream_t st, const SweepArgs &a);
+cudaError_t launch_tile(int kind, dim3 grid, cudaStream_t st, const SweepArgs &a, const BandArgs *band);
+template <int S>
+int tile_blocks_per_sm(int kind);
 template <int S>
 cudaError_t launch_hyp(int kind, int n, cudaStream_t st, const HypArgs &a);
 template <int S>
@@ -40,7 +43,8 @@ template <int Kind>
 int batch_mixed_blocks_per_sm(bool plain);
 cudaError_t dispatch_batch_mixed(int kind, bool plain, int blocks, cudaStream_t st, const BatchArgs &b);
 int dispatch_batch_mixed_blocks_per_sm(int kind, bool plain);
-cudaError_t dispatch_tile(int S, int kind, dim3 grid, cudaStream_t st, const SweepArgs &a);
+cudaError_t dispatch_tile(int S, int kind, dim3 grid, cudaStream_t st, const SweepArgs &a, const BandArgs *band);
+int dispatch_tile_blocks_per_sm(int S, int kind);
 cudaError_t dispatch_batch(int S, int kind, bool plain, int blocks, cudaStream_t st, const BatchArgs &b);
 int dispatch_batch_blocks_per_sm(int S, int kind, bool plain);
 cudaError_t dispatch_hyp(int S, int kind, int n, cudaStream_t st, const HypArgs &a);

@@ -11,7 +11,7 @@
 // reference moments are computed once per visit; the inner loop then
 // evaluates each hypothesis over the 36 taps and S sources with S independent
 // accumulation chains (recomputing each tap's bilateral weight, one MUFU.EX2
-// shared by the sources).  From 8 sources the CTA also stages the row and
+// shared by the sources).  From 9 sources the CTA also stages the row and
 // column factors of the warp (see stage_factors).
 #pragma once
 
@@ -430,6 +430,42 @@ template <int S, class Img, bool Plain>
 __global__ void __launch_bounds__(kThreads, tile_min_blocks<S>()) tile_kernel(const __grid_constant__ SweepArgs a) {
     extern __shared__ float4 tile[];
     tile_body<S, Img, Plain, ParamAccess>(a, blockIdx.x, blockIdx.y, tile);
+}
+
+// Banded tile order (BandArgs): the same tile visit in a persistent grid.
+// Tiles of one half-sweep never depend on each other, so any order gives
+// the same result; no CTA waits on another (one atomic per tile taken, at
+// most n_bands more when bands run out).
+template <int S, class Img, bool Plain>
+__global__ void __launch_bounds__(kThreads, tile_min_blocks<S>())
+    tile_kernel_banded(const __grid_constant__ SweepArgs a, const __grid_constant__ BandArgs b) {
+    extern __shared__ float4 tile[];
+    __shared__ int s_tile;
+    unsigned smid;
+    asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+    int band = (int)(smid % (unsigned)b.n_bands), exhausted = 0;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            int t = -1;
+            while (exhausted < b.n_bands) {
+                const int k = (int)atomicAdd(b.ctr + band, 1u);
+                const int start = band * b.per_band;
+                if (k < b.per_band && start + k < b.n_tiles) {
+                    t = start + k;
+                    break;
+                }
+                band = band + 1 == b.n_bands ? 0 : band + 1;
+                ++exhausted;
+            }
+            s_tile = t;
+        }
+        __syncthreads();
+        const int t = s_tile;
+        if (t < 0) return;
+        const int tx = t / b.tiles_y;
+        tile_body<S, Img, Plain, ParamAccess>(a, tx, t - tx * b.tiles_y, tile);
+        __syncthreads();  // before the next tile replaces the staged tile and s_tile
+    }
 }
 
 // Batched executor: a persistent grid walks a device queue of (request,

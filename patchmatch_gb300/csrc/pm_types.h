@@ -54,6 +54,18 @@ struct SweepArgs {
 
 static_assert(sizeof(SweepArgs) % 16 == 0, "SweepArgs is copied as 16-byte words");
 
+// Tile order of the banded (persistent) tile kernel: tiles in column-major
+// order are split into n_bands bands of per_band tiles, one per SM; each CTA
+// takes the next tile of its own SM's band with one atomic (so the CTAs
+// resident on an SM visit vertically adjacent tiles and share their source
+// footprints in L1) and moves on to the following bands when its own is
+// exhausted.  ctr holds one counter per band, zero before the launch.
+struct BandArgs {
+    unsigned int *ctr;
+    int n_bands, per_band, n_tiles, tiles_y;
+    int blocks;  // persistent grid: n_bands x resident CTAs per SM
+};
+
 // Arguments of the batched executor (one phase over many requests).
 struct BatchArgs {
     const SweepArgs *args;   // per request (mode/colour/sweep taken from here)
