@@ -66,8 +66,8 @@ constexpr int kMaxBands = 1024;  // counters of the banded tile order (one per S
 // The banded tile order (BandArgs) pays when the sources' texture rows are
 // wide: the CTAs resident on an SM then overflow L1 with unrelated tiles'
 // footprints.  Measured, 8 sweeps: 3840x1920 FP16 textures 4-8 sources
-// 1-6 % faster, 2880x1440 FP16 6 sources 1 % faster, 3840x1920 u8 8 sources
-// 3 % faster; below 30 KB of source row bytes (1920x960 at any format and
+// 1-5 % faster, 2880x1440 FP16 6 sources 1 % faster, 3840x1920 u8 8 sources
+// 2 % faster; below 30 KB of source row bytes (1920x960 at any format and
 // count, 2400x1200 FP16, 3840x1920 u8 up to 6 sources) even or 1-4 % slower,
 // where L1 already holds the footprints (95 % hit rate at 1920x960 u8).
 constexpr size_t kBandedMinRowBytes = 30000;
@@ -293,7 +293,7 @@ int ensure_textures(pm_request *r) {
 // 4-6 % slower banded at 1920x960).
 void set_tile_order(pm_request *r) {
     r->banded_blocks = 0;
-    if (r->ctx->n_sm <= 0 || r->ctx->n_sm > kMaxBands || r->prm.sampler != PM_SAMPLER_TEXTURE) return;
+    if (r->ctx->n_sm <= 0 || r->ctx->n_sm > kMaxBands / 2 || r->prm.sampler != PM_SAMPLER_TEXTURE) return;
     const size_t texel = r->prm.image_format == PM_IMAGE_F16 ? 2 : 1;
     if ((size_t)r->W * texel * (size_t)r->S < kBandedMinRowBytes) return;
     const int bps = pm::dispatch_tile_blocks_per_sm(r->S, pm::image_kind(r->prm.image_format, r->prm.sampler));
@@ -310,11 +310,13 @@ int launch_tile(pm_request *r, int mode, int colour, int sweep) {
     pm::BandArgs band{};
     const pm::BandArgs *bp = nullptr;
     if (r->banded_blocks > 0) {
+        const int n_sm = r->ctx->n_sm, segs = (n_sm + (int)grid.x - 1) / (int)grid.x;
         band.ctr = r->band_ctr;
-        band.n_bands = r->ctx->n_sm;
-        band.n_tiles = (int)(grid.x * grid.y);
-        band.per_band = (band.n_tiles + band.n_bands - 1) / band.n_bands;
+        band.tiles_x = (int)grid.x;
         band.tiles_y = (int)grid.y;
+        band.per_band = ((int)grid.y + segs - 1) / segs;
+        band.n_bands = (int)grid.x * segs;  // < tiles_x + n_sm <= kMaxBands
+        band.n_home = n_sm;
         band.blocks = r->banded_blocks;
         PM_CUDA(r->ctx, cudaMemsetAsync(r->band_ctr, 0, sizeof(unsigned) * band.n_bands, r->stream));
         bp = &band;

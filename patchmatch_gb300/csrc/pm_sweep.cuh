@@ -443,15 +443,15 @@ __global__ void __launch_bounds__(kThreads, tile_min_blocks<S>())
     __shared__ int s_tile;
     unsigned smid;
     asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
-    int band = (int)(smid % (unsigned)b.n_bands), exhausted = 0;
+    int band = (int)(smid % (unsigned)b.n_home), exhausted = 0;
     for (;;) {
         if (threadIdx.x == 0) {
             int t = -1;
             while (exhausted < b.n_bands) {
                 const int k = (int)atomicAdd(b.ctr + band, 1u);
-                const int start = band * b.per_band;
-                if (k < b.per_band && start + k < b.n_tiles) {
-                    t = start + k;
+                const int col = band % b.tiles_x, row = (band / b.tiles_x) * b.per_band + k;
+                if (k < b.per_band && row < b.tiles_y) {
+                    t = row * b.tiles_x + col;
                     break;
                 }
                 band = band + 1 == b.n_bands ? 0 : band + 1;
@@ -462,8 +462,8 @@ __global__ void __launch_bounds__(kThreads, tile_min_blocks<S>())
         __syncthreads();
         const int t = s_tile;
         if (t < 0) return;
-        const int tx = t / b.tiles_y;
-        tile_body<S, Img, Plain, ParamAccess>(a, tx, t - tx * b.tiles_y, tile);
+        const int ty = t / b.tiles_x;
+        tile_body<S, Img, Plain, ParamAccess>(a, t - ty * b.tiles_x, ty, tile);
         __syncthreads();  // before the next tile replaces the staged tile and s_tile
     }
 }

@@ -54,16 +54,19 @@ struct SweepArgs {
 
 static_assert(sizeof(SweepArgs) % 16 == 0, "SweepArgs is copied as 16-byte words");
 
-// Tile order of the banded (persistent) tile kernel: tiles in column-major
-// order are split into n_bands bands of per_band tiles, one per SM; each CTA
-// takes the next tile of its own SM's band with one atomic (so the CTAs
-// resident on an SM visit vertically adjacent tiles and share their source
-// footprints in L1) and moves on to the following bands when its own is
-// exhausted.  ctr holds one counter per band, zero before the launch.
+// Tile order of the banded (persistent) tile kernel.  Band b is a segment of
+// one tile column: column b % tiles_x, rows [seg * per_band, (seg + 1) *
+// per_band) with seg = b / tiles_x, the column split into as many segments
+// as make at least one band per SM.  A CTA starts on band smid % n_home and
+// takes its next tile with one atomic, so the CTAs resident on an SM walk
+// down vertically adjacent tiles and share their source footprints in L1,
+// while all SMs stay near the same rows of their segments (the sources stay
+// L2-resident); exhausted bands pass the CTA on to the following ones.  ctr
+// holds one counter per band, zero before the launch.
 struct BandArgs {
     unsigned int *ctr;
-    int n_bands, per_band, n_tiles, tiles_y;
-    int blocks;  // persistent grid: n_bands x resident CTAs per SM
+    int n_bands, per_band, tiles_x, tiles_y, n_home;
+    int blocks;  // persistent grid: SMs x resident CTAs per SM
 };
 
 // Arguments of the batched executor (one phase over many requests).
