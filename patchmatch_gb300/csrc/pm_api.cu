@@ -166,6 +166,22 @@ int validate_size(pm_ctx *ctx, int W, int H, int S) {
 
 }  // namespace
 
+int pmi::tile_band(pm_request *r, dim3 grid, cudaStream_t st, pm::BandArgs *band, const pm::BandArgs **out) {
+    *out = nullptr;
+    if (r->banded_blocks <= 0) return PM_OK;
+    const int n_sm = r->ctx->n_sm, segs = (n_sm + (int)grid.x - 1) / (int)grid.x;
+    band->ctr = r->band_ctr;
+    band->tiles_x = (int)grid.x;
+    band->tiles_y = (int)grid.y;
+    band->per_band = ((int)grid.y + segs - 1) / segs;
+    band->n_bands = (int)grid.x * segs;  // < tiles_x + n_sm <= kMaxBands
+    band->n_home = n_sm;
+    band->blocks = r->banded_blocks;
+    PM_CUDA(r->ctx, cudaMemsetAsync(r->band_ctr, 0, sizeof(unsigned) * band->n_bands, st));
+    *out = band;
+    return PM_OK;
+}
+
 void pmi::link_prior(pm_request *r, const pm_request *prior, const pm_result *res) {
     const auto drop = [r](std::vector<pm_request *> &v) { v.erase(std::remove(v.begin(), v.end(), r), v.end()); };
     if (r->prior) drop(r->prior->dependents);
@@ -309,18 +325,8 @@ int launch_tile(pm_request *r, int mode, int colour, int sweep) {
     const dim3 grid = pm::tile_grid(r->W, r->H);
     pm::BandArgs band{};
     const pm::BandArgs *bp = nullptr;
-    if (r->banded_blocks > 0) {
-        const int n_sm = r->ctx->n_sm, segs = (n_sm + (int)grid.x - 1) / (int)grid.x;
-        band.ctr = r->band_ctr;
-        band.tiles_x = (int)grid.x;
-        band.tiles_y = (int)grid.y;
-        band.per_band = ((int)grid.y + segs - 1) / segs;
-        band.n_bands = (int)grid.x * segs;  // < tiles_x + n_sm <= kMaxBands
-        band.n_home = n_sm;
-        band.blocks = r->banded_blocks;
-        PM_CUDA(r->ctx, cudaMemsetAsync(r->band_ctr, 0, sizeof(unsigned) * band.n_bands, r->stream));
-        bp = &band;
-    }
+    const int rc = pmi::tile_band(r, grid, r->stream, &band, &bp);
+    if (rc) return rc;
     cudaError_t e = pm::dispatch_tile(r->S, kind, grid, r->stream, a, bp);
     r->ctx->launches++;
     if (e != cudaSuccess) return fail(r->ctx, PM_ECUDA, "tile kernel launch: %s", cudaGetErrorString(e));

@@ -149,7 +149,12 @@ int batch_enqueue(pm_batch *b) {
                 a.mode = ph < 2 ? pm::kModeScore : pm::kModeSweep;
                 a.colour = ph < 2 ? ph : (ph - 2) & 1;
                 a.sweep = ph < 2 ? 0 : (ph - 2) >> 1;
-                cudaError_t e = pm::dispatch_tile(r->S, kind, pm::tile_grid(r->W, r->H), bs, a, nullptr);
+                const dim3 grid = pm::tile_grid(r->W, r->H);
+                pm::BandArgs band{};
+                const pm::BandArgs *bp = nullptr;
+                const int rc = pmi::tile_band(r, grid, bs, &band, &bp);
+                if (rc) return rc;
+                cudaError_t e = pm::dispatch_tile(r->S, kind, grid, bs, a, bp);
                 if (e != cudaSuccess) return fail(ctx, PM_ECUDA, "tile launch: %s", cudaGetErrorString(e));
                 ++launches;
             }
@@ -200,7 +205,12 @@ int batch_enqueue(pm_batch *b) {
                     a.mode = mode;
                     a.colour = colour;
                     a.sweep = sweep;
-                    cudaError_t e = pm::dispatch_tile(g.S, g.kind, pm::tile_grid(a.W, a.H), st, a, nullptr);
+                    const dim3 grid = pm::tile_grid(a.W, a.H);
+                    pm::BandArgs band{};
+                    const pm::BandArgs *bp = nullptr;
+                    const int rc = pmi::tile_band(g.members[m], grid, st, &band, &bp);
+                    if (rc) return rc;
+                    cudaError_t e = pm::dispatch_tile(g.S, g.kind, grid, st, a, bp);
                     if (e != cudaSuccess) return fail(ctx, PM_ECUDA, "tile launch: %s", cudaGetErrorString(e));
                     ++launches;
                 }

@@ -119,6 +119,10 @@ PM_INTERNAL void fill_args(pm_request *r);
 PM_INTERNAL int check_views(pm_request *r);
 // Enqueue the post-filter of a request on `st` (its own stream when null).
 PM_INTERNAL int enqueue_post(pm_request *r, cudaStream_t st = nullptr);
+// The band arguments of the request's tile order for one launch of `grid`
+// on `st`, with the band counters reset there first; *out is null when the
+// request runs one CTA per tile.
+PM_INTERNAL int tile_band(pm_request *r, dim3 grid, cudaStream_t st, pm::BandArgs *band, const pm::BandArgs **out);
 // Replace the prior links of r (request or retained result, at most one set),
 // keeping the priors' dependent lists in step.
 PM_INTERNAL void link_prior(pm_request *r, const pm_request *prior, const pm_result *res);

@@ -108,9 +108,9 @@ def test_request_in_a_batch_cannot_be_destroyed(ctx):
 def test_banded_tile_order_equals_one_cta_per_tile(ctx, fmt):
     """Wide texture-sampled requests (source row bytes W x texel bytes x S of
     at least 30,000: here 2048 x 2 x 8 for FP16, 3840 x 1 x 8 for u8) run their
-    sweeps in the banded persistent tile order; the per-request-launch batch
-    executor runs one CTA per tile.  Tiles of a half-sweep are independent, so
-    the maps are identical bit for bit."""
+    sweeps in the banded persistent tile order; the persistent batch executor
+    takes (request, tile) items from its own queue in raster order.  Tiles of
+    a half-sweep are independent, so the maps are identical bit for bit."""
     W = 2048 if fmt == native.IMAGE_F16 else 3840
     H, S = W // 2, 8
     req = scene.make_request(scene.ROOM_OBJECTS, W, H, S, seed=31)
@@ -120,7 +120,7 @@ def test_banded_tile_order_equals_one_cta_per_tile(ctx, fmt):
     r.run()
     banded = r.read(raw=True)
     b = native.Batch(ctx, [r])
-    b.set_executor(native.BATCH_LAUNCHES, 1)
+    b.set_executor(native.BATCH_PERSISTENT, 1)
     b.run()
     b.synchronize()
     per_tile = r.read(raw=True)
