@@ -31,19 +31,19 @@ cudaError_t tile_launch(dim3 grid, cudaStream_t st, const SweepArgs &a, const Ba
 template <class Img>
 cudaError_t tile_smem_attr() {
     constexpr int dyn = (int)tile_kernel_smem<PM_INST_S>();
-    constexpr int blocks = tile_min_blocks<PM_INST_S>();
+    constexpr int blocks = tile_min_blocks<PM_INST_S>(), pblocks = persistent_min_blocks<PM_INST_S>();
     cudaError_t e = cudaFuncSetAttribute(tile_kernel<PM_INST_S, Img, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
     e = e ? e : cudaFuncSetAttribute(tile_kernel<PM_INST_S, Img, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
     e = e ? e : prefer_l1(tile_kernel<PM_INST_S, Img, false>, dyn, blocks);
     e = e ? e : prefer_l1(tile_kernel<PM_INST_S, Img, true>, dyn, blocks);
-    e = e ? e : prefer_l1(batch_kernel<PM_INST_S, Img, false>, dyn, blocks);
-    e = e ? e : prefer_l1(batch_kernel<PM_INST_S, Img, true>, dyn, blocks);
+    e = e ? e : prefer_l1(batch_kernel<PM_INST_S, Img, false>, dyn, pblocks);
+    e = e ? e : prefer_l1(batch_kernel<PM_INST_S, Img, true>, dyn, pblocks);
     e = e ? e : cudaFuncSetAttribute(tile_kernel_banded<PM_INST_S, Img, false>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
     e = e ? e : cudaFuncSetAttribute(tile_kernel_banded<PM_INST_S, Img, true>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
-    e = e ? e : prefer_l1(tile_kernel_banded<PM_INST_S, Img, false>, dyn, blocks);
-    return e ? e : prefer_l1(tile_kernel_banded<PM_INST_S, Img, true>, dyn, blocks);
+    e = e ? e : prefer_l1(tile_kernel_banded<PM_INST_S, Img, false>, dyn, pblocks);
+    return e ? e : prefer_l1(tile_kernel_banded<PM_INST_S, Img, true>, dyn, pblocks);
 }
 
 template <class Img>

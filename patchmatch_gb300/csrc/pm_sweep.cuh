@@ -168,9 +168,15 @@ struct Park {
 
 // Resident CTAs per SM the register allocation targets: 3 (80 registers)
 // holds up to 8 sources with the visit state parked; more sources need the
-// 128-register budget.
+// 128-register budget.  The one-CTA-per-tile kernel runs 4 (64 registers, no
+// spills) up to 4 sources, where the extra warps hide more texture latency
+// (measured, 8 sweeps at 1920x960: 2 sources 3 %, 3 sources 1 %, 4 sources
+// 3 % faster; 5-6 sources spill and run 1-3 % slower).  The persistent
+// kernels (banded, batched) keep 3: at 64 registers they spill.
 template <int S>
-constexpr int tile_min_blocks() { return S <= 8 ? 3 : 2; }
+constexpr int persistent_min_blocks() { return S <= 8 ? 3 : 2; }
+template <int S>
+constexpr int tile_min_blocks() { return S <= 4 ? 4 : persistent_min_blocks<S>(); }
 
 // Smoothness factor f in [0, 1] of a propagated plane p against the pixel's
 // current plane h and its depth before propagation (PatchMatchCuda.cu:322-337).
@@ -437,7 +443,7 @@ __global__ void __launch_bounds__(kThreads, tile_min_blocks<S>()) tile_kernel(co
 // the same result; no CTA waits on another (one atomic per tile taken, at
 // most n_bands more when bands run out).
 template <int S, class Img, bool Plain>
-__global__ void __launch_bounds__(kThreads, tile_min_blocks<S>())
+__global__ void __launch_bounds__(kThreads, persistent_min_blocks<S>())
     tile_kernel_banded(const __grid_constant__ SweepArgs a, const __grid_constant__ BandArgs b) {
     extern __shared__ float4 tile[];
     __shared__ int s_tile;
@@ -476,7 +482,7 @@ __global__ void __launch_bounds__(kThreads, tile_min_blocks<S>())
 // other (a half-sweep reads only the other colour), so no CTA waits on
 // another; phases are separated by kernel boundaries.
 template <int S, class Img, bool Plain>
-__global__ void __launch_bounds__(kThreads, tile_min_blocks<S>()) batch_kernel(const __grid_constant__ BatchArgs b) {
+__global__ void __launch_bounds__(kThreads, persistent_min_blocks<S>()) batch_kernel(const __grid_constant__ BatchArgs b) {
     extern __shared__ float4 tile[];
     __shared__ SweepArgs sa;
     __shared__ int s_item;
