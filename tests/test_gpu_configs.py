@@ -1,0 +1,110 @@
+"""Full-run parity on the benchmark workloads, at the method's tolerance:
+>= 99 % of valid pixels within 1 % relative depth.
+
+"Valid" is what the densifier hands on: the post-filtered depth map
+(DepthmapEstimator::PostProcess, depthmap.cc:1169-1208) is non-zero.  The
+oracle's raw maps go through the oracle's restatement of that filter, the
+GPU's through its own; a pixel counts when both keep it.  Coverage (the
+fraction kept) is reported beside the agreement and is asserted not to
+shrink, so the filter cannot buy agreement by rejecting pixels.
+
+Both samplers are checked.  The exact sampler is compared with the FP64
+oracle (exact bilinear weights).  The texture sampler is compared with the
+oracle's model of the texture unit (coordinates rounded to 1/256 texel,
+PatchMatchCuda.cu:136-137 samples through the same unit).
+
+1920x960 with 6 sources is too large for the oracle in a test, so it runs on a
+band of rows.  A half-sweep moves information at most 3 rows (neighbour
+offsets +-1, +-3, PatchMatchCuda.cu:287-296), so after 16 half-sweeps a row
+more than 48 rows inside the band has seen exactly what it sees in a full
+run; only those rows are compared.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from patchmatch_gb300 import native, scene
+
+pytestmark = pytest.mark.gpu
+
+SWEEPS = 8
+REACH = 3 * 2 * SWEEPS  # rows a full run's state can move during SWEEPS red+black sweeps
+
+
+def _request(ctx, req, **kw):
+    p = native.default_params(iterations=SWEEPS, **kw)
+    r = ctx.request(req.W, req.H, req.n_src, p)
+    r.set_views([v.gray_u8 for v in req.views], req.R, req.t)
+    return r
+
+
+def _agreement(g_raw, g_filt, o_raw, o_filt, rows, gt):
+    """(agreement on pixels both filters keep, coverage of each, raw agreement
+    on interior pixels, accuracy of each against the truth)."""
+    H, W = g_raw.shape
+    interior = np.zeros((H, W), bool)
+    interior[6:H - 5, 6:W - 5] = True
+    sel = np.zeros((H, W), bool)
+    sel[rows] = True
+    sel &= interior
+    both = sel & (g_filt > 0) & (o_filt > 0)
+    rel = np.abs(g_filt - o_filt) / np.where(o_filt > 0, o_filt, 1)
+    agree_valid = (rel[both] < 0.01).mean()
+    cov_g = (g_filt > 0)[sel].mean()
+    cov_o = (o_filt > 0)[sel].mean()
+    agree_raw = (np.abs(g_raw - o_raw) / o_raw < 0.01)[sel].mean()
+    acc = lambda d: (np.abs(d - gt) / gt < 0.01)[sel & (d > 0)].mean()
+    return agree_valid, cov_g, cov_o, agree_raw, acc(g_filt), acc(o_filt)
+
+
+def _oracle_filtered(req, raw):
+    d, _ = O.postprocess(req.views[0].gray_u8.astype(np.float32), raw["depth"], raw["score"])
+    return d
+
+
+@pytest.mark.parametrize("sampler", [native.SAMPLER_EXACT, native.SAMPLER_TEXTURE])
+def test_cfg1_full_run_matches_oracle(ctx, sampler):
+    """512x256 room, 4 sources, 8 sweeps, fold rule, Philox seed 0: the whole
+    image against the oracle."""
+    req = scene.config_request(1, seed=0)
+    r = _request(ctx, req, sampler=sampler)
+    r.run()
+    g_raw, g_filt = r.read(raw=True), r.read()
+    r.close()
+    interp = O.INTERP_EXACT if sampler == native.SAMPLER_EXACT else O.INTERP_TEX8_RN
+    o = O.patchmatch(O.Views.from_request(req), O.cost_params(interp=interp), iterations=SWEEPS)
+    o_filt = _oracle_filtered(req, o)
+    a, cg, co, araw, accg, acco = _agreement(g_raw["depth"], g_filt["depth"], o["depth"], o_filt,
+                                             slice(None), req.views[0].depth)
+    print(f"cfg1 sampler={sampler}: valid-pixel agreement within 1% {a:.5f} (coverage gpu {cg:.4f} oracle {co:.4f}); "
+          f"raw interior agreement {araw:.5f}; accuracy 1% gpu {accg:.4f} oracle {acco:.4f}")
+    assert a >= 0.99
+    assert cg >= co - 0.01
+    assert accg >= acco - 0.01
+
+
+@pytest.mark.parametrize("sampler", [native.SAMPLER_EXACT, native.SAMPLER_TEXTURE])
+def test_cfg2_band_matches_oracle(ctx, sampler):
+    """1920x960 room with boxes and a cylinder, 6 sources, top-3 view
+    selection, 8 sweeps: the GPU's full run against the oracle run on a
+    144-row band, compared on the 48 rows the band's edges cannot reach."""
+    req = scene.config_request(2, seed=0)
+    r = _request(ctx, req, sampler=sampler, combine=native.COMBINE_TOPK, top_k=3)
+    r.run()
+    g_raw, g_filt = r.read(raw=True), r.read()
+    r.close()
+    H = req.H
+    lo = H // 2 - 24 - REACH
+    hi = H // 2 + 24 + REACH
+    interp = O.INTERP_EXACT if sampler == native.SAMPLER_EXACT else O.INTERP_TEX8_RN
+    o = O.patchmatch(O.Views.from_request(req), O.cost_params(interp=interp, combine=O.COMBINE_TOPK, top_k=3),
+                     iterations=SWEEPS, row_lo=lo, row_hi=hi)
+    o_filt = _oracle_filtered(req, o)
+    rows = slice(lo + REACH, hi - REACH)
+    a, cg, co, araw, accg, acco = _agreement(g_raw["depth"], g_filt["depth"], o["depth"], o_filt, rows,
+                                             req.views[0].depth)
+    print(f"cfg2 band sampler={sampler}: valid-pixel agreement within 1% {a:.5f} (coverage gpu {cg:.4f} "
+          f"oracle {co:.4f}); raw agreement {araw:.5f}; accuracy 1% gpu {accg:.4f} oracle {acco:.4f}")
+    assert a >= 0.99
+    assert cg >= co - 0.01
+    assert accg >= acco - 0.01

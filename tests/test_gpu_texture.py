@@ -91,15 +91,23 @@ def test_matches_reference_kernel_scores():
         ij = np.stack([ii, jj], 1).astype(np.int32)
         g, _ = r.score_hypotheses(ij, gold["planes"][ii, jj])
         r.close()
-    err = np.abs(g - gold["scores"][ii, jj])
+    ref = gold["scores"][ii, jj]
+    err = np.abs(g - ref)
+    within = (err <= 1e-5 * np.maximum(1.0, np.abs(ref))).mean()
     print(f"gpu texture vs reference kernel: median {np.median(err):.2e} p99 {np.quantile(err, .99):.2e} "
-          f"max {err.max():.2e}")
+          f"max {err.max():.2e}; within 1e-5 relative {within:.5f}")
     assert np.median(err) < 1e-5 and np.quantile(err, 0.99) < 1e-4
+    # the rest are samples whose coordinates fall on the other side of a
+    # 1/256-texel step of the texture unit's weights (our FP32 angle
+    # arithmetic against the reference's atan2f/asinf)
+    assert within >= 0.95
 
 
 def test_full_run_agrees_with_oracle_tex8(ctx):
     """8 sweeps at 256x128, 4 sources: the texture-sampled GPU run and the
-    oracle run with texture weights converge to the same depths."""
+    oracle run with texture weights converge to the same depths (raw maps,
+    every interior pixel; the post-filtered comparison at the benchmark
+    sizes is in test_gpu_configs.py)."""
     req = scene.make_request(scene.ROOM, 256, 128, 4, seed=13)
     r = _tex_request(ctx, req, iterations=8, postprocess=0)
     r.run()
@@ -112,7 +120,7 @@ def test_full_run_agrees_with_oracle_tex8(ctx):
     acc_g = (np.abs(g["depth"] - gt) / gt < 0.05)[interior].mean()
     acc_o = (np.abs(o["depth"] - gt) / gt < 0.05)[interior].mean()
     print(f"agreement {agree:.4f} gpu-acc5% {acc_g:.4f} oracle-acc5% {acc_o:.4f}")
-    assert agree >= 0.90
+    assert agree >= 0.98
     assert acc_g >= acc_o - 0.02
     r.close()
 
