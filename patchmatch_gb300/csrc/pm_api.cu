@@ -695,6 +695,10 @@ int pm_create(int device, size_t hbm_budget_bytes, pm_ctx **out) {
     e = e ? e : pm::configure_tile<8>();
     e = e ? e : pm::configure_tile<9>();
     e = e ? e : pm::configure_tile<10>();
+    e = e ? e : pm::configure_batch_mixed<pm::kImageQuadU8>();
+    e = e ? e : pm::configure_batch_mixed<pm::kImageQuadF16>();
+    e = e ? e : pm::configure_batch_mixed<pm::kImageTexU8>();
+    e = e ? e : pm::configure_batch_mixed<pm::kImageTexF16>();
     if (e != cudaSuccess) {
         cudaStreamDestroy(ctx->stream);
         delete ctx;

@@ -75,6 +75,13 @@ cudaError_t launch_batch_mixed<PM_MIXED_KIND>(bool plain, int blocks, cudaStream
 }
 
 template <>
+cudaError_t configure_batch_mixed<PM_MIXED_KIND>() {
+    constexpr int dyn = (int)tile_kernel_smem_max();
+    cudaError_t e = cudaFuncSetAttribute(batch_mixed_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
+    return e ? e : cudaFuncSetAttribute(batch_mixed_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
+}
+
+template <>
 int batch_mixed_blocks_per_sm<PM_MIXED_KIND>(bool plain) {
     int n = 0;
     if (plain)

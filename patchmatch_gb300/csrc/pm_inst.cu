@@ -36,6 +36,8 @@ cudaError_t tile_smem_attr() {
     e = e ? e : cudaFuncSetAttribute(tile_kernel<PM_INST_S, Img, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
     e = e ? e : prefer_l1(tile_kernel<PM_INST_S, Img, false>, dyn, blocks);
     e = e ? e : prefer_l1(tile_kernel<PM_INST_S, Img, true>, dyn, blocks);
+    e = e ? e : cudaFuncSetAttribute(batch_kernel<PM_INST_S, Img, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
+    e = e ? e : cudaFuncSetAttribute(batch_kernel<PM_INST_S, Img, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
     e = e ? e : prefer_l1(batch_kernel<PM_INST_S, Img, false>, dyn, pblocks);
     e = e ? e : prefer_l1(batch_kernel<PM_INST_S, Img, true>, dyn, pblocks);
     e = e ? e : cudaFuncSetAttribute(tile_kernel_banded<PM_INST_S, Img, false>,

@@ -41,6 +41,8 @@ template <int Kind>
 cudaError_t launch_batch_mixed(bool plain, int blocks, cudaStream_t st, const BatchArgs &b);
 template <int Kind>
 int batch_mixed_blocks_per_sm(bool plain);
+template <int Kind>
+cudaError_t configure_batch_mixed();  // dynamic shared-memory limit of the current device
 cudaError_t dispatch_batch_mixed(int kind, bool plain, int blocks, cudaStream_t st, const BatchArgs &b);
 int dispatch_batch_mixed_blocks_per_sm(int kind, bool plain);
 cudaError_t dispatch_tile(int S, int kind, dim3 grid, cudaStream_t st, const SweepArgs &a, const BandArgs *band);

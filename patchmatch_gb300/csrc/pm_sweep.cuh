@@ -55,16 +55,27 @@ __device__ __forceinline__ void load_tile(float4 *tile, const float2 *row_trig, 
 // registers without spilling.  The centre bearing is re-read from the tile.
 constexpr int kParkSlots = 17;
 
-// Dynamic shared memory of tile_kernel: the staged tile, the parked state
-// and the warp factors (per source: A of both column parities, B of both
-// signs); the rest of the SM's unified L1/shared storage stays L1 for the
-// texture samples, whose hit rate sets the kernel's speed: the total per SM
-// is kept under the 100 KB carveout where the sources allow.
+// Propagation candidates of a pixel visit: the neighbours (0,1), (1,0),
+// (0,-1), (-1,0), (0,3), (3,0), (0,-3), (-3,0) (PatchMatchCuda.cu:305).
+constexpr int kNbr = 8;
+
+// Dynamic shared memory of tile_kernel: the staged tile, the parked state,
+// the scratch of the speculative propagation pass (see tile_body) and the
+// warp factors (per source: A of both column parities, B of both signs); the
+// rest of the SM's unified L1/shared storage stays L1 for the texture
+// samples, whose hit rate sets the kernel's speed.
 constexpr int kFactorA = 2 * kTileCols;  // (column parity, same-colour column)
 constexpr int kFactorB = 2 * kTileRows;  // (sign, row)
-// Byte offsets: tile, parked state, factors.
+// Byte offsets: tile, parked state, speculative pass (reference moments per
+// pixel, candidate scores and best sources per (candidate, pixel), the
+// (pixel, candidate) work list, per-warp scan totals), factors.
 constexpr size_t kSmemPark = sizeof(float4) * kTilePos;
-constexpr size_t kSmemFactors = kSmemPark + sizeof(float) * kParkSlots * kThreads;
+constexpr size_t kSpecMom = kSmemPark + sizeof(float) * kParkSlots * kThreads;
+constexpr size_t kSpecRes = kSpecMom + sizeof(float) * 3 * kThreads;
+constexpr size_t kSpecBest = kSpecRes + sizeof(float) * kNbr * kThreads;
+constexpr size_t kSpecList = kSpecBest + sizeof(int8_t) * kNbr * kThreads;
+constexpr size_t kSpecTot = kSpecList + sizeof(uint16_t) * kNbr * kThreads;
+constexpr size_t kSmemFactors = (kSpecTot + sizeof(int) * (kThreads / 32) + 15) / 16 * 16;
 constexpr size_t kTileSmemBytes = kSmemFactors;
 template <int S>
 __host__ __device__ constexpr size_t tile_kernel_smem() {
@@ -76,9 +87,8 @@ __host__ __device__ constexpr size_t tile_kernel_smem_max() {
                ? tile_kernel_smem<PM_MAX_SOURCES>()
                : tile_kernel_smem<PM_FACTOR_MAX_SOURCES>();
 }
-// The mixed batch kernel launches without raising its dynamic shared-memory
-// limit, so every layout stays within the default 48 KB.
-static_assert(tile_kernel_smem_max() <= 48 * 1024, "tile layout exceeds the default dynamic shared memory");
+// Three CTAs of the largest layout fit one SM's 228 KB of shared memory.
+static_assert(3 * (tile_kernel_smem_max() + 1024) <= 228 * 1024, "tile layout exceeds the per-SM shared memory");
 
 // Ask for the smallest shared-memory carveout that holds `blocks` CTAs of
 // `kernel` with `dyn` bytes of dynamic shared memory, leaving the rest of the
@@ -194,12 +204,155 @@ __device__ __forceinline__ float smoothness_factor(float px, float py, float pz,
     return __fmul_rn(__fsub_rn(1.0f, dsf), __fsub_rn(1.0f, psf));
 }
 
+// Geometry of same-colour pixel p (0..255) of the tile at (i0, x0): image
+// position, its centre entry in the staged tile, the first tap row and column
+// of its window in the tile, and the column parity of the staged entries on
+// its tap rows (rows rbase + 2 m1 of the tile: image rows i0 - 5 + rbase + 2 m1).
+struct TilePixel {
+    int i, j, ctr_e, rbase, cbase, pa;
+    __device__ __forceinline__ TilePixel(int p, int i0, int x0, int colour, int ph) {
+        const int ty = p >> 5, lane = p & 31;
+        i = i0 + ty;
+        const int par = (i + colour) & 1;
+        j = x0 + 2 * lane + par;
+        ctr_e = (ty + kHaloMax) * kTileCols + ((2 * lane + par + kHaloMax) >> 1);
+        rbase = ty + kHaloMax - ph;
+        cbase = lane + ((kHaloMax - ph) >> 1);
+        pa = (i0 + rbase + colour) & 1;
+    }
+};
+
+// Image index of propagation candidate n of pixel (i, j).
+__device__ __forceinline__ size_t nbr_index(int n, int i, int j, int W) {
+    const int sel = n & 3, far = (n >> 2) ? 3 : 1;
+    const int di = (sel == 1) ? far : (sel == 3 ? -far : 0);
+    const int dj = (sel == 0) ? far : (sel == 2 ? -far : 0);
+    return (size_t)(i + di) * W + (j + dj);
+}
+
+// Window moments of plane (px, py, pz) at a pixel: the 36 taps x S sources of
+// the plane-induced warp (PatchMatchCuda.cu:100-157), one tap row and column
+// at a time from the staged tile.
+template <int S, class Img, class Acc, class A>
+__device__ __forceinline__ void accumulate_plane(TapAccum<S, Img, Acc> &acc, const A &a, const float4 *tile,
+                                                 const float4 *fac, int rbase, int cbase, int pa, float Ic, float px,
+                                                 float py, float pz) {
+    const int nt = a.patch_half + 1, ph = a.patch_half;
+    const float shift = Img::shift_for(Ic);
+    const float halfW = fmaf(0.5f, Acc::val(a.Wf), Img::kCoordOffset);
+    const float halfH = fmaf(0.5f, Acc::val(a.Hf), Img::kCoordOffset);
+    acc.zero();
+#pragma unroll 1
+    for (int m1 = 0; m1 < nt; ++m1) {
+        const int tr = rbase + 2 * m1;
+        const float4 *trow = tile + tr * kTileCols + cbase;
+        const int k1 = 2 * m1 - ph;
+        const float dk1 = (float)(k1 * k1) * Acc::val(a.ndf);
+#pragma unroll 1
+        for (int m2 = 0; m2 < nt; ++m2) {
+            const float4 e = trow[m2];
+            const int k2 = 2 * m2 - ph;
+            const float xs = e.w - Ic;
+            const float w = bilateral_weight(xs, Acc::val(a.ncf), fmaf((float)(k2 * k2), Acc::val(a.ndf), dk1));
+            if constexpr (factored_warp<S>()) {
+                const float s = fmaf(px, e.x, fmaf(py, e.y, pz * e.z));
+                const float4 *fa = fac + pa * kTileCols + cbase + m2;
+                const float4 *fb = fac + S * kFactorA + (s < 0.0f ? kTileRows : 0) + tr;
+                acc.add_rot(a.P, a.src, Acc::val(a.Wf), Acc::val(a.Hf), halfW, halfH, shift, fabsf(s),
+                            [&](int r) {
+                                const float4 ca = fa[r * kFactorA], rb = fb[r * kFactorB];
+                                return make_float3(fmaf(rb.w, ca.x, rb.x), fmaf(rb.w, ca.y, rb.y),
+                                                   fmaf(rb.w, ca.z, rb.z));
+                            },
+                            w, xs);
+            } else {
+                acc.add_bearing(a.P, a.src, Acc::val(a.Wf), Acc::val(a.Hf), halfW, halfH, shift, px, py, pz, e.x, e.y,
+                                e.z, w, xs);
+            }
+        }
+    }
+}
+
+// Exclusive prefix sum of one count per thread over the CTA; *total gets the
+// sum.  tot: one int per warp in shared memory.  Contains one barrier; the
+// caller separates consecutive calls by at least one more.
+__device__ __forceinline__ int cta_exclusive_scan(int cnt, int *tot, int *total) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int x = cnt;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, d);
+        if (lane >= d) x += y;
+    }
+    if (lane == 31) tot[wid] = x;
+    __syncthreads();
+    int off = 0, sum = 0;
+#pragma unroll
+    for (int w = 0; w < kThreads / 32; ++w) {
+        const int t = tot[w];
+        off += (w < wid) ? t : 0;
+        sum += t;
+    }
+    *total = sum;
+    return off + x - cnt;
+}
+
+// One speculative round of the propagation pass: every thread lists the
+// candidates in `need` (bit n = candidate n of its pixel), the CTA scores all
+// listed (pixel, candidate) pairs with every thread taking the next pair, and
+// the scores (NCC combination before the smoothness factor) and best sources
+// land in res/res_best[n][pixel].  All threads of the CTA call it together.
+template <int S, class Img, class Acc, class A>
+__device__ __forceinline__ void spec_round(const A &a, const float4 *tile, const float4 *fac, unsigned char *smem,
+                                           int i0, int x0, unsigned need) {
+    const float *mom = reinterpret_cast<const float *>(smem + kSpecMom);
+    float *res = reinterpret_cast<float *>(smem + kSpecRes);
+    int8_t *res_best = reinterpret_cast<int8_t *>(smem + kSpecBest);
+    uint16_t *list = reinterpret_cast<uint16_t *>(smem + kSpecList);
+    int total;
+    int k = cta_exclusive_scan(__popc(need), reinterpret_cast<int *>(smem + kSpecTot), &total);
+    for (unsigned m = need; m; m &= m - 1) list[k++] = (uint16_t)((threadIdx.x << 3) | (__ffs(m) - 1));
+    __syncthreads();
+#pragma unroll 1
+    for (int base = 0; base < total; base += kThreads) {
+        const int q = base + (int)threadIdx.x;
+        if (q < total) {
+            const int e = list[q], p = e >> 3, n = e & 7;
+            const TilePixel g(p, i0, x0, a.colour, a.patch_half);
+            const float4 np = a.plane[nbr_index(n, g.i, g.j, a.W)];
+            TapAccum<S, Img, Acc> acc;
+            accumulate_plane(acc, a, tile, fac, g.rbase, g.cbase, g.pa, tile[g.ctr_e].w, np.x, np.y, np.z);
+            float sep[S], cum[S];
+            source_nccs(acc, mom[p], mom[kThreads + p], mom[2 * kThreads + p], a.combine, sep, cum);
+            int hb;
+            res[n * kThreads + p] = combine_scores<S>(sep, cum, a.combine, a.top_k, &hb);
+            res_best[n * kThreads + p] = (int8_t)hb;
+        }
+    }
+    __syncthreads();
+}
+
 // One tile visit: CTA-wide tile staging (one barrier), then per-thread work.
 // `a` is the kernel's parameter block (single-request launches) or a copy in
 // shared memory (the batched executor); (bx, by) is the tile index.
+//
+// Red-black sweeps (PatchMatchCuda.cu:287-404) visit each pixel's eight
+// propagation candidates in order, then six refinements.  The refinements are
+// scored for every pixel, but a candidate is scored only while it can still
+// be accepted (2 f > score, see below), so pixels need 0-8 propagation costs
+// and a warp that walks its lanes' candidates in step spends as long as its
+// busiest lane.  The sweep therefore scores propagation speculatively: the
+// CTA lists every (pixel, candidate) pair that passes the test in the pixel's
+// state before propagation and scores the list with all its threads; each
+// pixel then replays its candidates in order with those scores.  A candidate
+// that passes only after an earlier one was taken (the test depends on the
+// current plane and score) is listed in a further round, together with every
+// later candidate that passes in the new state; rounds repeat until no pixel
+// waits.  Every decision is the one the in-order walk takes, so results are
+// unchanged; only the assignment of costs to threads differs.
 template <int S, class Img, bool Plain, class Acc, class A>
 __device__ __forceinline__ void tile_body(const A &a, int bx, int by, float4 *tile) {
-    const int tid = threadIdx.x, lane = tid & 31, ty = tid >> 5;
+    const int tid = threadIdx.x;
     const int x0 = bx * kTileW, i0 = by * kTileH;
     unsigned char *const smem = reinterpret_cast<unsigned char *>(tile);
     float4 *const fac = reinterpret_cast<float4 *>(smem + kSmemFactors);
@@ -208,35 +361,35 @@ __device__ __forceinline__ void tile_body(const A &a, int bx, int by, float4 *ti
     __syncthreads();
 
     const int W = a.W, H = a.H, ph = a.patch_half;
-    int i = i0 + ty;
-    const int p = (i + a.colour) & 1;
-    int j = x0 + 2 * lane + p;
-    if (i < ph + 1 || i > H - ph - 1 || j < ph + 1 || j > W - ph - 1) return;  // PatchMatchCuda.cu:283
+    const TilePixel g(tid, i0, x0, a.colour, ph);
+    int i = g.i, j = g.j;
+    const bool active = !(i < ph + 1 || i > H - ph - 1 || j < ph + 1 || j > W - ph - 1);  // PatchMatchCuda.cu:283
+    constexpr bool plain = Plain;  // PM_PROPAGATION_PLAIN (a separate instantiation)
+    const bool spec = a.mode == kModeSweep && !plain;
+    if (!active && !spec) return;
 
-    const int ctr_e = (ty + kHaloMax) * kTileCols + ((2 * lane + p + kHaloMax) >> 1);
+    const int ctr_e = g.ctr_e;
+    const int rbase = g.rbase, cbase = g.cbase, pa = g.pa;
     const float4 ctr = tile[ctr_e];
     float bxc = ctr.x, byc = ctr.y, bzc = ctr.z;
     const float Ic = ctr.w;
     const int nt = ph + 1;
-    const int cbase = lane + ((kHaloMax - ph) >> 1);
-    const int rbase = ty + kHaloMax - ph;
-    // column parity of the staged entries on this pixel's tap rows
-    // (rows rbase + 2 m1 of the tile: image rows i0 - 5 + rbase + 2 m1)
-    const int pa = (i0 + rbase + a.colour) & 1;
 
     // hypothesis-independent moments of the reference window; the bilateral
     // weights are recomputed per tap in the hypothesis loop (one MUFU.EX2 per
     // tap, shared by all sources) rather than held in shared memory
     float sw = 0.f, swx = 0.f, swxx = 0.f;
-    for (int m1 = 0; m1 < nt; ++m1) {
-        const int k1 = 2 * m1 - ph;
-        for (int m2 = 0; m2 < nt; ++m2) {
-            const int k2 = 2 * m2 - ph;
-            const float xs = tile[(rbase + 2 * m1) * kTileCols + cbase + m2].w - Ic;
-            const float w = bilateral_weight(xs, a.ncf, (float)(k1 * k1 + k2 * k2) * a.ndf);
-            sw += w;
-            swx = fmaf(w, xs, swx);
-            swxx = fmaf(w * xs, xs, swxx);
+    if (active) {
+        for (int m1 = 0; m1 < nt; ++m1) {
+            const int k1 = 2 * m1 - ph;
+            for (int m2 = 0; m2 < nt; ++m2) {
+                const int k2 = 2 * m2 - ph;
+                const float xs = tile[(rbase + 2 * m1) * kTileCols + cbase + m2].w - Ic;
+                const float w = bilateral_weight(xs, a.ncf, (float)(k1 * k1 + k2 * k2) * a.ndf);
+                sw += w;
+                swx = fmaf(w, xs, swx);
+                swxx = fmaf(w * xs, xs, swxx);
+            }
         }
     }
 
@@ -246,29 +399,86 @@ __device__ __forceinline__ void tile_body(const A &a, int bx, int by, float4 *ti
         cand = a.cand[idx];
         if (!(cand.w > 0.0f)) return;  // no candidate for this pixel
     }
-    const float4 cur = a.plane[idx];
-    constexpr bool plain = Plain;  // PM_PROPAGATION_PLAIN (a separate instantiation)
+    const float4 cur = active ? a.plane[idx] : make_float4(0.f, 0.f, 0.f, 0.f);
     if (a.mode == kModeSweep && plain && cur.w == 0.0f) return;  // ignored pixel (depthmap.cc:1007-1010)
-    float score = a.score[idx];
-    int best = a.best[idx];
+    float score = active ? a.score[idx] : 0.0f;
+    int best = active ? a.best[idx] : 0;
     float hx = cur.x, hy = cur.y, hz = cur.z;   // plane_*_hyp of the reference
     float curr_depth = cur.w;
     float cand_w = cand.w;
+    bool moved = false;    // plain propagation: a neighbour's plane was taken
+    int h = 0;
+
+    if (spec) {
+        // ---- speculative propagation pass (see above) ----
+        float *mom = reinterpret_cast<float *>(smem + kSpecMom);
+        mom[tid] = sw;
+        mom[kThreads + tid] = swx;
+        mom[2 * kThreads + tid] = swxx;
+        const float *res = reinterpret_cast<const float *>(smem + kSpecRes);
+        const int8_t *res_best = reinterpret_cast<const int8_t *>(smem + kSpecBest);
+        // candidates passing 2 f > score (the in-order walk's test) for m >= from
+        // in the current state that are not scored yet
+        auto passing = [&](int from, unsigned have) {
+            unsigned m = 0;
+            if (active)
+                for (int n = from; n < kNbr; ++n) {
+                    if ((have >> n) & 1u) continue;
+                    const float4 np = a.plane[nbr_index(n, i, j, W)];
+                    const float f = smoothness_factor(np.x, np.y, np.z, hx, hy, hz, bxc, byc, bzc, curr_depth);
+                    if (2.0f * f > score) m |= 1u << n;
+                }
+            return m;
+        };
+        unsigned need = passing(0, 0u), avail = 0;
+        int n = 0;
+        const Park park(smem);
+#pragma unroll 1
+        while (__syncthreads_or(need != 0)) {
+            park.save(hx, hy, hz, score, best | (n << 8) | (int)(avail << 16) | (int)(need << 24), curr_depth);
+            spec_round<S, Img, Acc>(a, tile, fac, smem, i0, x0, need);
+            {
+                int st;
+                park.load(hx, hy, hz, score, st, curr_depth);
+                best = (int)(int8_t)(st & 0xff);
+                n = (st >> 8) & 0xff;
+                avail = ((unsigned)st >> 16) & 0xffu;
+                avail |= ((unsigned)st >> 24) & 0xffu;
+                const float4 c = tile[ctr_e];
+                bxc = c.x;
+                byc = c.y;
+                bzc = c.z;
+            }
+            need = 0;
+            if (active) {
+                // replay in order with the scores at hand (PatchMatchCuda.cu:305-337)
+#pragma unroll 1
+                for (; n < kNbr; ++n) {
+                    const float4 np = a.plane[nbr_index(n, i, j, W)];
+                    const float f = smoothness_factor(np.x, np.y, np.z, hx, hy, hz, bxc, byc, bzc, curr_depth);
+                    if (!(2.0f * f > score)) continue;  // cannot be accepted (also when f is NaN)
+                    if (!((avail >> n) & 1u)) break;   // passes only in the state reached so far
+                    const float sc = __fmul_rn(res[n * kThreads + tid], f);
+                    if (sc > score) { hx = np.x; hy = np.y; hz = np.z; score = sc; best = res_best[n * kThreads + tid]; }
+                }
+                if (n < kNbr) need = (1u << n) | passing(n + 1, avail);
+            }
+        }
+        if (!active) return;
+        h = kNbr;  // refinements follow
+    }
+
     float cx = hx, cy = hy, cz = hz, current_depth = curr_depth;
     float depth_hyp = 0.f;
-    const float shift = Img::shift_for(Ic);
-    const float halfW = fmaf(0.5f, a.Wf, Img::kCoordOffset), halfH = fmaf(0.5f, a.Hf, Img::kCoordOffset);
     const int nh = a.mode == kModeSweep ? 14 : 1;
 
     // Propagated planes are scored as NCC x f with a smoothness factor
     // f in [0, 1] that does not depend on the cost (PatchMatchCuda.cu:322-337).
     // A candidate with 2 f <= score cannot be accepted by any combined score
     // <= 2 (the exact NCC is bounded by 1), so its cost is not evaluated.
-    // Each lane walks its own pixel's hypotheses in order and passes over such
-    // candidates: a warp evaluates as many costs as its busiest lane needs.
-    int h = 0;
+    // In the plain (host-variant) propagation every neighbour is scored
+    // unless its depth is 0, in order, by each lane for its own pixel.
     int kr = 0;            // plain propagation: refinements tried so far (their ranges shrink only when tried)
-    bool moved = false;    // plain propagation: a neighbour's plane was taken
 #pragma unroll 1
     while (true) {
         float px = 0.f, py = 0.f, pz = 0.f, f = 1.0f;
@@ -279,12 +489,8 @@ __device__ __forceinline__ void tile_body(const A &a, int bx, int by, float4 *ti
                 px = hx; py = hy; pz = hz;
             } else if (a.mode == kModeSeed) {
                 px = cand.x; py = cand.y; pz = cand.z;
-            } else if (h < 8) {
-                // neighbours (0,1),(1,0),(0,-1),(-1,0),(0,3),(3,0),(0,-3),(-3,0) (PatchMatchCuda.cu:305)
-                const int sel = h & 3, far = (h >> 2) ? 3 : 1;
-                const int di = (sel == 1) ? far : (sel == 3 ? -far : 0);
-                const int dj = (sel == 0) ? far : (sel == 2 ? -far : 0);
-                const float4 np = a.plane[(size_t)(i + di) * W + (j + dj)];
+            } else if (h < kNbr) {
+                const float4 np = a.plane[nbr_index(h, i, j, W)];
                 px = np.x; py = np.y; pz = np.z;
                 if (plain) {
                     if (np.w == 0.0f) continue;  // ignored neighbour (depthmap.cc:1018-1021)
@@ -293,7 +499,7 @@ __device__ __forceinline__ void tile_body(const A &a, int bx, int by, float4 *ti
                     if (!(2.0f * f > score)) continue;  // cannot be accepted (also when f is NaN)
                 }
             } else {
-                const int t = h - 8;
+                const int t = h - kNbr;
                 if (t == 0) {
                     // current depth after propagation (PatchMatchCuda.cu:340-341); the
                     // host variant keeps the stored depth unless a neighbour was taken
@@ -346,36 +552,7 @@ __device__ __forceinline__ void tile_body(const A &a, int bx, int by, float4 *ti
 
         // ---- cost of hypothesis (px, py, pz) ----
         TapAccum<S, Img, Acc> acc;
-        acc.zero();
-#pragma unroll 1
-        for (int m1 = 0; m1 < nt; ++m1) {
-            const int tr = rbase + 2 * m1;
-            const float4 *trow = tile + tr * kTileCols + cbase;
-            const int k1 = 2 * m1 - ph;
-            const float dk1 = (float)(k1 * k1) * a.ndf;
-#pragma unroll 1
-            for (int m2 = 0; m2 < nt; ++m2) {
-                const float4 e = trow[m2];
-                const int k2 = 2 * m2 - ph;
-                const float xs = e.w - Ic;
-                const float w = bilateral_weight(xs, Acc::val(a.ncf), fmaf((float)(k2 * k2), Acc::val(a.ndf), dk1));
-                if constexpr (factored_warp<S>()) {
-                    const float s = fmaf(px, e.x, fmaf(py, e.y, pz * e.z));
-                    const float4 *fa = fac + pa * kTileCols + cbase + m2;
-                    const float4 *fb = fac + S * kFactorA + (s < 0.0f ? kTileRows : 0) + tr;
-                    acc.add_rot(a.P, a.src, Acc::val(a.Wf), Acc::val(a.Hf), halfW, halfH, shift, fabsf(s),
-                                [&](int r) {
-                                    const float4 ca = fa[r * kFactorA], rb = fb[r * kFactorB];
-                                    return make_float3(fmaf(rb.w, ca.x, rb.x), fmaf(rb.w, ca.y, rb.y),
-                                                       fmaf(rb.w, ca.z, rb.z));
-                                },
-                                w, xs);
-                } else {
-                    acc.add_bearing(a.P, a.src, Acc::val(a.Wf), Acc::val(a.Hf), halfW, halfH, shift, px, py, pz, e.x,
-                                    e.y, e.z, w, xs);
-                }
-            }
-        }
+        accumulate_plane(acc, a, tile, fac, rbase, cbase, pa, Ic, px, py, pz);
         {
             int st, ij;
             park.load(hx, hy, hz, cx, cy, cz, score, current_depth, depth_hyp, f, sw, swx, swxx, curr_depth, cand_w, st,
@@ -404,7 +581,7 @@ __device__ __forceinline__ void tile_body(const A &a, int bx, int by, float4 *ti
             if (sc > score) {  // the host seeding rule (depthmap.cc:483-487)
                 cx = px; cy = py; cz = pz; score = sc; current_depth = cand_w; best = hb;
             }
-        } else if (h < 8) {
+        } else if (h < kNbr) {
             sc = __fmul_rn(sc, f);
             if (sc > score) { hx = px; hy = py; hz = pz; score = sc; best = hb; moved = true; }
         } else {
