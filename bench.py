@@ -2,16 +2,24 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-A step densifies one keyframe: Philox initialisation, init scoring, 8
-red-black sweeps (propagation + 6 refinements per pixel visit) and the
-post-filter.  The metric is Mpix*views/s = (W*H/1e6) * sources / seconds per
-keyframe (whole job: summed over GPUs; N > 1 runs independent replicas).
+A step is one keyframe through the whole path, as the reference's
+densification and fusion threads run it per keyframe in steady state:
+Philox initialisation, init scoring, 8 red-black sweeps (propagation + 6
+refinements per pixel visit, top-3 view selection), the post-filter, the
+geometric-consistency filter of the keyframe's depth against four resident
+neighbour depth maps (1 px round trip, 0.01 relative depth, 3 consistent
+views of 5) and point fusion of the cleaned map against the four neighbour
+maps (0.08 relative depth, the reference's example configuration).  The
+metric is Mpix*views/s = (W*H/1e6) * sources / seconds per keyframe (whole
+job: summed over GPUs; N > 1 runs independent replicas).
 
   value : device-resident inputs, CUDA-event time of the step on the
-          context's stream; L2 is flushed (256 MB write) between steps.
-  e2e   : the same step through the public C ABI (pm_densify) from pinned
-          host buffers: host->device copy of the 7 images and device->host
-          copy of the depth and score maps are inside the timed region.
+          request's stream; L2 is flushed (256 MB write) between steps.
+  e2e   : the same step through the public C ABI from pinned host buffers:
+          host->device copy of the 7 images, then pm_request_run,
+          pm_filter_consistency_device and pm_fuse_device, then the
+          device->host copy of the cleaned depth, the score map and the fused
+          points, all inside the timed region.
 
 served: the same densifier behind the served request loop (pm_server) on a
           keyframe stream along a trajectory through a hall of boxes, mixed
@@ -32,7 +40,6 @@ from __future__ import annotations
 import argparse
 import json
 import os
-import re
 import statistics
 import subprocess
 import sys
@@ -47,8 +54,14 @@ W, H, S, SWEEPS = 1920, 960, 6, 8
 METRIC = "Mpix·views/s and p50/p99 keyframe latency, served vs plain at ≤1% depth error"
 UNIT = "Mpix·views/s"
 WORKLOAD = ("plain PatchMatch, one 1920x960 u8 equirect keyframe + 6 sources per step, 8 red-black sweeps, "
-            "11x11 window at stride 2, fold view combination, room + 5 boxes + cylinder scene")
+            "11x11 window at stride 2, top-3 view selection, post-filter, geometric-consistency filter "
+            "(1 px round trip, 0.01 relative depth, 3 of 5 views) and point fusion (0.08) against 4 resident "
+            "neighbour depth maps, room + 5 boxes + cylinder scene")
+TOP_K = 3
+CLEAN_THR, CLEAN_PX, CLEAN_MIN = 0.01, 1.0, 3
+FUSE_THR = 0.08
 FLOP_PER_SAMPLE = 40  # algorithmic FP32 work of one (pixel, hypothesis, source, tap) sample
+SFU_PER_SAMPLE = 4    # special-function operations of one sample (rcp, rsqrt and the two angles)
 
 
 def _mpix_views(ms: float) -> float:
@@ -153,23 +166,42 @@ def _hbm_view(traffic, launch_ms):
             "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"}
 
 
-def _traffic_from_profile():
-    """DRAM bytes per sweep launch from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", "tile_kernel_1920x960x6.md")
-    if not os.path.exists(path):
+# DRAM bytes of one sweep launch of this workload, from one ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum), valid only for the kernel
+# sources it was measured on: a different build reports null rather than a
+# stale figure.
+TRAFFIC_NCU = {"bytes_per_launch": None, "sources_sha256": None}
+KERNEL_SOURCES = ("patchmatch_gb300/csrc/pm_sweep.cuh", "patchmatch_gb300/csrc/pm_device.cuh",
+                  "patchmatch_gb300/csrc/pm_inst.cu", "patchmatch_gb300/csrc/pm_types.h")
+
+
+def kernel_sources_sha256() -> str:
+    import hashlib
+    h = hashlib.sha256()
+    for f in KERNEL_SOURCES:
+        with open(os.path.join(ROOT, f), "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()
+
+
+def _traffic():
+    if TRAFFIC_NCU["bytes_per_launch"] is None or TRAFFIC_NCU["sources_sha256"] != kernel_sources_sha256():
         return None
-    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", open(path).read())
-    return float(m.group(1)) if m else None
+    return TRAFFIC_NCU["bytes_per_launch"]
 
 
 def cpu_sample(target_s: float = 12.0, threads: int = 0):
-    """Reference per-pixel algorithm (oracle, reference float arithmetic) on a
-    band of rows of the workload, 8 sweeps; returns Mpix*views/s and the band."""
+    """The reference's per-keyframe host work on the workload: the per-pixel
+    densification (oracle, reference float arithmetic, top-3 views, OpenMP)
+    on a band of rows, 8 sweeps, scaled to the full keyframe, plus the
+    consistency filter and fusion of full-size maps (the reference runs both
+    single-threaded, depthmap.cc:1320-1377,1535-1696).  Returns Mpix*views/s,
+    the band rows, seconds per keyframe, threads and the seconds the sample took."""
     from oracle import oracle as O
     from patchmatch_gb300 import scene
     req = scene.config_request(2, seed=0)
     V = O.Views.from_request(req)
-    cp = O.cost_params(arith=O.ARITH_F32_REF)
+    cp = O.cost_params(arith=O.ARITH_F32_REF, combine=O.COMBINE_TOPK, top_k=TOP_K)
     threads = threads or os.cpu_count() or 1
     # calibrate on 4 rows x 1 sweep
     r0 = H // 2
@@ -178,10 +210,16 @@ def cpu_sample(target_s: float = 12.0, threads: int = 0):
     rows = int(max(2, min(H - 20, target_s / (per_row_sweep * SWEEPS))))
     lo = max(6, r0 - rows // 2)
     res = O.patchmatch(V, cp, iterations=SWEEPS, row_lo=lo, row_hi=lo + rows, threads=threads)
-    secs = res["seconds"]
-    value = (W * rows / 1e6) * S / secs
-    return value, rows, secs, threads, V, req
-
+    dens = res["seconds"] * H / rows
+    maps = [np.ascontiguousarray(v.depth, np.float32) for v in req.views[:5]]
+    t0 = time.perf_counter()
+    cleaned = O.clean([maps[1], maps[2], maps[0], maps[3], maps[4]], req.R[[1, 2, 0, 3, 4]], req.t[[1, 2, 0, 3, 4]],
+                      center=2, thr=CLEAN_THR, min_consistent=CLEAN_MIN, reproj_px=CLEAN_PX)
+    O.prune([cleaned] + maps[1:5], req.R[:5], req.t[:5], None, FUSE_THR)
+    post = time.perf_counter() - t0
+    secs = dens + post
+    value = (W * H / 1e6) * S / secs
+    return value, rows, secs, threads, res["seconds"] + post
 
 def reference_gpu_sweep_ms():
     """The reference's own CUDA path (PatchMatchCuda.cu compiled unmodified,
@@ -212,13 +250,14 @@ def run_reference(args):
     steps = []
     info = None
     for k in range(args.warmup + args.steps):
-        v, rows, secs, threads, _, _ = cpu_sample(target_s=args.cpu_seconds)
+        v, rows, _, threads, wall_s = cpu_sample(target_s=args.cpu_seconds)
         if k >= args.warmup:
-            steps.append((v, secs))
+            steps.append((v, wall_s))
         info = (rows, threads)
     value = statistics.median(v for v, _ in steps)
     rows, threads = info
-    sample = f"rows {H // 2 - rows // 2}..+{rows} of the 1920x960x6 workload, all {SWEEPS} sweeps"
+    sample = (f"densification of rows {H // 2 - rows // 2}..+{rows} of the 1920x960x6 workload (all {SWEEPS} "
+              "sweeps, top-3) scaled to the keyframe, plus the full-size consistency filter and fusion")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * statistics.median(s for _, s in steps),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -357,11 +396,11 @@ def run_pipeline(native, scene, ctx, local: int, steps: int) -> dict:
 
     def clean():
         ctx.check(L.pm_filter_consistency(ctx.h, W, H, 5, C.cast(ptrs, C.c_void_p), Rd.ctypes.data, td.ctypes.data,
-                                          2, 0.01, 3, 0.0, cleaned.ctypes.data))
+                                          2, CLEAN_THR, CLEAN_MIN, CLEAN_PX, cleaned.ctypes.data))
 
     def fuse():
         ctx.check(L.pm_fuse(ctx.h, W, H, 5, C.cast(ptrs, C.c_void_p), Rd.ctypes.data, td.ctypes.data,
-                            bgr.ctypes.data, 0.02, pruned.ctypes.data, C.byref(pts)))
+                            bgr.ctypes.data, FUSE_THR, pruned.ctypes.data, C.byref(pts)))
 
     out = {}
     for name, fn in (("filter", clean), ("fuse", fuse)):
@@ -375,9 +414,42 @@ def run_pipeline(native, scene, ctx, local: int, steps: int) -> dict:
                 ts.append(time.perf_counter() - t0)
         out[f"{name}_ms"] = 1e3 * statistics.median(ts)
     out["fused_points"] = int(pts.count)
+    # the same calls on device buffers (pm_filter_consistency_device,
+    # pm_fuse_device), CUDA events on the context's stream
+    dev = torch.device("cuda", local)
+    dd = [torch.from_numpy(x).to(dev) for x in depths]
+    dw = [torch.empty_like(x) for x in dd]
+    dclean = torch.empty((H, W), dtype=torch.float32, device=dev)
+    dpr = torch.empty((H, W), dtype=torch.float32, device=dev)
+    dxyz = torch.empty((H * W, 3), dtype=torch.float32, device=dev)
+    dcnt = torch.zeros(1, dtype=torch.int32, device=dev)
+    wsb = native.fuse_workspace_bytes(W, H)
+    wsbuf = torch.empty(wsb + 256, dtype=torch.uint8, device=dev)
+    wsp = (wsbuf.data_ptr() + 255) & ~255
+    cst = torch.cuda.ExternalStream(ctx.stream_handle)
+    for name, fn in (("filter_device", lambda: ctx.filter_consistency_device(
+            [x.data_ptr() for x in dd], W, H, R, t, 2, CLEAN_THR, dclean.data_ptr(), CLEAN_MIN, CLEAN_PX)),
+                     ("fuse_device", lambda: ctx.fuse_device([x.data_ptr() for x in dw], W, H, R, t, FUSE_THR,
+                                                             dpr.data_ptr(), dxyz.data_ptr(), dcnt.data_ptr(), wsp,
+                                                             wsb))):
+        ts = []
+        for k in range(max(3, steps) + 1):
+            with torch.cuda.stream(cst):
+                for a, b in zip(dw, dd):
+                    a.copy_(b)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(cst)
+            fn()
+            with torch.cuda.stream(cst):
+                e1.record(cst)
+            e1.synchronize()
+            if k:
+                ts.append(e0.elapsed_time(e1))
+        out[f"{name}_ms"] = statistics.median(ts)
     out["workload"] = ("1920x960, 5 depth maps (0.4 % noise, 10 % holes); filter: centre map 2, 1 % depth "
-                       "threshold, 3 consistent views; fuse: head map 0 against 1-4, 2 % threshold; one C ABI "
-                       "call each with host buffers in and out (copies included, buffers preallocated)")
+                       "threshold, 1 px round trip, 3 consistent views; fuse: head map 0 against 1-4, 8 % "
+                       "threshold; one C ABI call each, host buffers in and out (copies included, buffers "
+                       "preallocated), and the device-buffer calls (CUDA events)")
     return out
 
 
@@ -458,6 +530,72 @@ def run_batched(native, scene, ctx, local: int, args) -> dict:
                         "between the forms"}
 
 
+class KeyframeStep:
+    """One keyframe through the path on the device: pm_request_run
+    (densification + post-filter), pm_filter_consistency_device against four
+    resident neighbour depth maps (window order n0 n1 keyframe n2 n3, centre
+    2) and pm_fuse_device of the cleaned map against the four neighbours (head
+    0), all on the request's stream.  The neighbours are sources 1-4 of the
+    request, each densified once beforehand with the other six views as its
+    sources; fusion edits later maps in place, so each step fuses fresh device
+    copies of them (copied on the stream inside the step)."""
+
+    def __init__(self, native, ctx, req, params, local):
+        import torch
+        self.torch, self.native, self.ctx = torch, native, ctx
+        dev = torch.device("cuda", local)
+        imgs = [np.ascontiguousarray(v.gray_u8) for v in req.views]
+        self.imgs = imgs
+        self.R, self.t = req.R, req.t
+        self.r = ctx.request(W, H, S, params)
+        self.r.set_views(imgs, req.R, req.t)
+        self.nbr = []
+        for q in (1, 2, 3, 4):
+            order = [q] + [k for k in range(S + 1) if k != q]
+            rq = ctx.request(W, H, S, native.default_params(iterations=params.iterations, combine=params.combine,
+                                                            top_k=params.top_k, seed=params.seed, keyframe_id=q))
+            rq.set_views([imgs[k] for k in order], req.R[order], req.t[order])
+            rq.run()
+            rq.synchronize()
+            self.nbr.append(torch.from_numpy(rq.read()["depth"]).to(dev))
+            rq.close()
+        self.work = [torch.empty_like(n) for n in self.nbr]
+        self.cleaned = torch.zeros((H, W), dtype=torch.float32, device=dev)
+        self.pruned = torch.zeros((H, W), dtype=torch.float32, device=dev)
+        self.xyz = torch.zeros((H * W, 3), dtype=torch.float32, device=dev)
+        self.ij = torch.zeros((H * W, 2), dtype=torch.int32, device=dev)
+        self.count = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.ws_bytes = native.fuse_workspace_bytes(W, H)
+        self.ws = torch.empty(self.ws_bytes + 256, dtype=torch.uint8, device=dev)
+        self.ws_ptr = (self.ws.data_ptr() + 255) & ~255
+        win = [1, 2, 0, 3, 4]
+        self.R_win, self.t_win = req.R[win], req.t[win]
+        self.R_fuse, self.t_fuse = req.R[:5], req.t[:5]
+        self.st = self.r.stream_handle
+        self.es = torch.cuda.ExternalStream(self.st)
+
+    def enqueue(self):
+        """The step, enqueued on the request's stream."""
+        torch = self.torch
+        self.r.run()
+        ptrs = [n.data_ptr() for n in self.nbr]
+        self.ctx.filter_consistency_device([ptrs[0], ptrs[1], self.r.depth_device_ptr, ptrs[2], ptrs[3]], W, H,
+                                           self.R_win, self.t_win, 2, CLEAN_THR, self.cleaned.data_ptr(),
+                                           min_consistent=CLEAN_MIN, reproj_px=CLEAN_PX, stream=self.st)
+        with torch.cuda.stream(self.es):
+            for w, n in zip(self.work, self.nbr):
+                w.copy_(n, non_blocking=True)
+        self.ctx.fuse_device([self.cleaned.data_ptr()] + [w.data_ptr() for w in self.work], W, H, self.R_fuse,
+                             self.t_fuse, FUSE_THR, self.pruned.data_ptr(), self.xyz.data_ptr(),
+                             self.count.data_ptr(), self.ws_ptr, self.ws_bytes, ij_ptr=self.ij.data_ptr(),
+                             stream=self.st)
+
+    def close(self):
+        self.r.close()
+        self.es = None
+        self.nbr = self.work = self.cleaned = self.pruned = self.xyz = self.ij = self.count = self.ws = None
+
+
 def run_ours(args):
     import torch
     rank, ws, local, dist = _dist()
@@ -465,17 +603,16 @@ def run_ours(args):
     from patchmatch_gb300 import native, scene
 
     req = scene.config_request(2, seed=rank)
-    imgs = [np.ascontiguousarray(v.gray_u8) for v in req.views]
     ctx = native.Context(local)
-    p = native.default_params(iterations=SWEEPS, seed=rank)
-    r = ctx.request(W, H, S, p)
-    r.set_views(imgs, req.R, req.t)
-    stream = torch.cuda.ExternalStream(r.stream_handle)
+    p = native.default_params(iterations=SWEEPS, seed=rank, combine=native.COMBINE_TOPK, top_k=TOP_K)
+    ks = KeyframeStep(native, ctx, req, p, local)
+    r = ks.r
+    stream = ks.es
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
 
     # --- device-resident steps ---
     for _ in range(args.warmup):
-        r.run()
+        ks.enqueue()
     r.synchronize()
     torch.cuda.synchronize()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
@@ -488,7 +625,7 @@ def run_ours(args):
             with torch.cuda.stream(stream):
                 flush.fill_(k & 0xFF)  # L2 flush between steps, outside the events
                 ev[k][0].record(stream)
-            r.run()
+            ks.enqueue()
             with torch.cuda.stream(stream):
                 ev[k][1].record(stream)
         r.synchronize()
@@ -500,8 +637,10 @@ def run_ours(args):
     ms_step = _allmax(dist, sum(ms) / len(ms))
     value = ws * _mpix_views(ms_step)
     lat = np.array(ms)
+    fused_points = int(ks.count.item())
+    cleaned_valid = float((ks.cleaned > 0).float().mean().item())
 
-    # --- dominant kernel: one red-black half-sweep, timed on the context stream ---
+    # --- dominant kernel: one red-black half-sweep, timed on the request's stream ---
     r.run()
     nhalf = 2 * SWEEPS
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -516,32 +655,56 @@ def run_ours(args):
     peak = ctx.probe_fp32_peak()
 
     # --- end to end through the C ABI from pinned host buffers ---
-    pin = [torch.from_numpy(im).pin_memory() for im in imgs]
+    pin = [torch.from_numpy(im).pin_memory() for im in ks.imgs]
     d_out = torch.empty((H, W), dtype=torch.float32).pin_memory()
     s_out = torch.empty((H, W), dtype=torch.float32).pin_memory()
+    n_pin = torch.empty(1, dtype=torch.int32).pin_memory()
+    xyz_pin = torch.empty((H * W, 3), dtype=torch.float32).pin_memory()
+    ij_pin = torch.empty((H * W, 2), dtype=torch.int32).pin_memory()
     import ctypes as C
-    views = (native.View * (S + 1))(*[native.make_view(pin[k].data_ptr(), req.R[k], req.t[k]) for k in range(S + 1)])
-    maps = native.Maps()
-    maps.depth = d_out.data_ptr()
-    maps.score = s_out.data_ptr()
     L = native.lib()
+    maps = native.Maps()
+    maps.score = s_out.data_ptr()
+
+    def e2e_step():
+        for k in range(S + 1):
+            ctx.check(L.pm_request_set_view(r.h, k, C.byref(native.make_view(pin[k].data_ptr(), req.R[k],
+                                                                              req.t[k]))))
+        ks.enqueue()
+        ctx.check(L.pm_request_read_async(r.h, C.byref(maps), 0))
+        with torch.cuda.stream(stream):
+            d_out.copy_(ks.cleaned, non_blocking=True)
+            n_pin.copy_(ks.count, non_blocking=True)
+        r.synchronize()
+        n = int(n_pin.item())
+        with torch.cuda.stream(stream):
+            xyz_pin[:n].copy_(ks.xyz[:n], non_blocking=True)
+            ij_pin[:n].copy_(ks.ij[:n], non_blocking=True)
+        r.synchronize()
+        return n
+
     for _ in range(max(1, args.warmup)):
-        ctx.check(L.pm_densify(ctx.h, W, H, views, S + 1, C.byref(p), C.byref(maps)))
+        e2e_step()
     _barrier(dist)
     e2e_t = []
+    n_pts = 0
     for _ in range(args.steps):
         flush.fill_(1)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        ctx.check(L.pm_densify(ctx.h, W, H, views, S + 1, C.byref(p), C.byref(maps)))
+        n_pts = e2e_step()
         e2e_t.append(time.perf_counter() - t0)
     e2e_ms = _allmax(dist, 1e3 * sum(e2e_t) / len(e2e_t))
     e2e_value = ws * _mpix_views(e2e_ms)
-    valid = float((d_out.numpy() > 0).mean())
+    e2e_d2h = int(2 * 4 * W * H + 4 + n_pts * (12 + 8))
     gt = req.views[0].depth
-    dn = d_out.numpy()
+    dn = d_out.numpy().copy()  # no view may keep the pinned buffer alive past the request's stream
     m = dn > 0
+    valid = float(m.mean())
     acc = float((np.abs(dn[m] - gt[m]) / gt[m] < 0.01).mean()) if m.any() else 0.0
+    filt = r.read()["depth"]
+    mf = filt > 0
+    acc_filt = float((np.abs(filt[mf] - gt[mf]) / gt[mf] < 0.01).mean()) if mf.any() else 0.0
 
     # two sources (the reference CUDA path's only configuration), per red+black sweep
     req2 = scene.make_request(scene.ROOM_OBJECTS, W, H, 2, seed=33, bmin=0.1, bmax=0.8)
@@ -568,15 +731,23 @@ def run_ours(args):
     served = None if args.no_served else run_served(native, scene, ctx, local, args)
     batched = None if args.no_batched else run_batched(native, scene, ctx, local, args)
     pipeline = run_pipeline(native, scene, ctx, local, args.steps)
-    traffic = _traffic_from_profile()
+    traffic = _traffic()
+    # the roofline terms of the cost kernel (samples/s): 40 FP32 flop, 4
+    # special-function operations and 1 bilinear fetch per sample
+    sfu = ctx.probe_sfu_peak()
+    tex = ctx.probe_tex_peak()
+    terms = {"fp32": peak * 1e12 / FLOP_PER_SAMPLE, "sfu": sfu * 1e9 / SFU_PER_SAMPLE, "tex": tex * 1e9}
+    binding = min(terms, key=terms.get)
+    samples_s = _samples_per_half_sweep() / (sweep_ms * 1e-3)
     line = None
     if rank == 0:
         cpu = None
         if not args.no_cpu and ws == 1:  # the CPU leg runs at N = 1 only
-            v, rows, secs, threads, _, _ = cpu_sample(target_s=args.cpu_seconds)
+            v, rows, secs, threads, _ = cpu_sample(target_s=args.cpu_seconds)
             cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                   "sample": f"{rows} rows x 1920 of the same workload, all {SWEEPS} sweeps, "
-                             f"{secs:.1f} s, reference float arithmetic (oracle), OpenMP"}
+                   "sample": f"densification of {rows} rows x 1920 of the same workload (all {SWEEPS} sweeps, "
+                             f"top-3, reference float arithmetic, OpenMP) scaled to the keyframe, plus the "
+                             f"full-size consistency filter and fusion: {secs:.1f} s per keyframe"}
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
@@ -586,14 +757,24 @@ def run_ours(args):
                        "l2": "flushed between steps (256 MB write outside the timed events)"},
             "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                            "form": "plain (one keyframe at a time)"},
-            "quality": {"valid_fraction": valid, "within_1pct_of_truth": acc},
+            "quality": {"cleaned_valid_fraction": valid, "cleaned_within_1pct_of_truth": acc,
+                        "postfiltered_valid_fraction": float(mf.mean()), "postfiltered_within_1pct_of_truth": acc_filt,
+                        "fused_points": fused_points},
             "e2e": {"value": e2e_value, "unit": UNIT, "ms_per_step": e2e_ms,
-                    "h2d_bytes_per_step": int((S + 1) * W * H), "d2h_bytes_per_step": int(2 * 4 * W * H)},
+                    "h2d_bytes_per_step": int((S + 1) * W * H), "d2h_bytes_per_step": e2e_d2h,
+                    "form": "images from pinned host memory -> pm_request_set_view, pm_request_run, "
+                            "pm_filter_consistency_device, pm_fuse_device -> cleaned depth, score and fused "
+                            "points (xyz, pixel) to pinned host memory"},
             "roofline": {"bound": "fp32", "kernel": "tile_kernel (red-black half-sweep)",
                          "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                          "peak_source": "in-run FFMA probe (pm_probe_fp32_peak); MEASURED_PEAKS.json has no FP32 figure",
                          "flop_per_sample": FLOP_PER_SAMPLE, "samples_per_launch": _samples_per_half_sweep(),
                          "launch_ms": sweep_ms, "traffic": traffic,
+                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of this build's "
+                                           "sweep kernel, null when the kernel sources differ from the profiled",
+                         "terms_samples_per_s": terms, "binding_term": binding,
+                         "achieved_samples_per_s": samples_s, "frac_of_binding": samples_s / terms[binding],
+                         "probes": {"fp32_tflops": peak, "sfu_gops": sfu, "tex_gfetches": tex},
                          "hbm_view": _hbm_view(traffic, sweep_ms)},
             "served": served,
             "batched": batched,
@@ -604,8 +785,15 @@ def run_ours(args):
             "gpu_launches": int(gpu_launches),
             "wall_s_timed_region": wall,
         }
-        print(json.dumps(line))
-    r.close()
+        print(json.dumps(line), flush=True)
+    # the pinned e2e buffers were copied on the request's stream: free them
+    # while that stream still exists (their allocator records events on it)
+    del pin, d_out, s_out, n_pin, xyz_pin, ij_pin
+    torch.cuda.synchronize()
+    del ev, e0, e1, stream
+    ks.close()
+    del ks
+    torch.cuda.synchronize()
     ctx.close()
     if dist is not None:
         dist.destroy_process_group()
@@ -635,4 +823,6 @@ def main():
 
 
 if __name__ == "__main__":
+    import faulthandler
+    faulthandler.enable()
     main()

@@ -166,6 +166,14 @@ void *pm_stream(const pm_ctx *ctx);
  * kernel on the context's stream; 1 FMA = 2 flop).  The densifier's cost
  * kernel is bounded by the FP32 pipe, so this is its roofline denominator. */
 int pm_probe_fp32_peak(pm_ctx *ctx, double *tflops);
+/* Measured special-function-unit throughput (approximate exponentials, one
+ * MUFU instruction each, like the cost kernel's reciprocals, reciprocal
+ * square roots and exponentials) in Gop/s, and bilinear texture-fetch
+ * throughput from an L1-resident u8 texture in Gfetch/s: the two other terms
+ * of the cost kernel's roofline (40 FP32 flop, 4 special-function operations
+ * and 1 bilinear fetch per sample). */
+int pm_probe_sfu_peak(pm_ctx *ctx, double *gops);
+int pm_probe_tex_peak(pm_ctx *ctx, double *gfetches);
 
 /* One keyframe, host buffers in and out (synchronous).  views[0] is the
  * reference keyframe, views[1..n_views-1] its sources (1..PM_MAX_SOURCES).
@@ -250,8 +258,8 @@ int pm_request_query(const pm_request *req);
 /* The request's own CUDA stream (a cudaStream_t): every request runs on its
  * own stream, so requests of one context overlap on the device. */
 void *pm_request_stream(const pm_request *req);
-/* Device pointer of the (filtered) depth map, H x W float, for chaining
- * into pm_filter/pm_fuse without a host round trip. */
+/* Device pointer of the (filtered) depth map, H x W float, for chaining into
+ * pm_filter_consistency_device / pm_fuse_device without a host round trip. */
 const float *pm_request_depth_device(const pm_request *req);
 
 /* Score n fixed plane hypotheses at pixels ij[2n] (row, col) against the
@@ -285,6 +293,34 @@ typedef struct {
  * Replaces DepthmapPruner::Prune (depthmap.cc:1535-1696). */
 int pm_fuse(pm_ctx *ctx, int width, int height, int n_views, float *const *depths, const double *R_cw,
             const double *t_cw, const uint8_t *bgr, float same_depth_threshold, float *pruned, pm_points *out);
+
+/* The same two stages on DEVICE buffers, chained after densification without
+ * a host round trip: depths[k] are device pointers (e.g. pm_request_depth_device
+ * of finished requests, or caller buffers) and every output is a device
+ * buffer.  Work is enqueued on `stream` (a cudaStream_t; NULL = the context's
+ * stream) and the call returns without synchronising; order the stream after
+ * the work that writes the inputs.  Neither call allocates, except that the
+ * context builds its bearing tables for an image size on the first use of that
+ * size.  Same kernels and results as the host-buffer calls.
+ * Replace DepthmapCleaner::Clean (depthmap.cc:1320-1377) and
+ * DepthmapPruner::Prune (depthmap.cc:1535-1696) for device-resident maps (the
+ * reference hands host cv::Mat copies between its threads,
+ * depthmap_computation_module.cc:396-412, dense_pointcloud_module.cc:115-175). */
+int pm_filter_consistency_device(pm_ctx *ctx, int width, int height, int n_views, const float *const *depths,
+                                 const double *R_cw, const double *t_cw, int center, float same_depth_threshold,
+                                 int min_consistent_views, float reproj_px, float *out, void *stream);
+/* Bytes of the fusion workspace for one image size (0 for invalid sizes). */
+size_t pm_fuse_workspace_bytes(int width, int height);
+/* Fusion on device maps: the later maps are edited in place as by pm_fuse;
+ * pruned (H x W), xyz (H*W x 3 floats, world frame), bgr_out (H*W x 3, may be
+ * NULL), ij (H*W x 2 int32 (row, col), may be NULL) and count (one unsigned)
+ * receive the results; bgr (device, may be NULL) is the head's colour image.
+ * workspace: a 256-byte aligned device block of pm_fuse_workspace_bytes bytes
+ * that no other call uses until this one has finished on the device. */
+int pm_fuse_device(pm_ctx *ctx, int width, int height, int n_views, float *const *depths, const double *R_cw,
+                   const double *t_cw, const uint8_t *bgr, float same_depth_threshold, float *pruned, float *xyz,
+                   uint8_t *bgr_out, int32_t *ij, unsigned *count, void *workspace, size_t workspace_bytes,
+                   void *stream);
 
 /* ---- served densification (a request loop over the calls above) ----
  * Keyframes are submitted as SLAM emits them (any thread).  A worker thread
@@ -359,7 +395,10 @@ int pm_server_destroy(pm_server *srv);
  * height <= PM_FUSE_NOALLOC_MAX_HEIGHT (larger sizes return PM_EINVAL).
  * The first call on each device looks up that array's device address
  * (cudaGetSymbolAddress) with the device current; make that first call before
- * any stream capture.  All calls on a device share the array: calls whose GPU
+ * any stream capture.  The first call for each image size on a device also
+ * copies that size's bearing tables from host memory into the array.  A launch
+ * error left pending by earlier work on the calling thread is cleared on entry
+ * (it is not reported as this call's).  All calls on a device share the array: calls whose GPU
  * work overlaps (e.g. on two streams) race and must be serialised by the
  * caller.  depths[k] (device, H x W floats, k = 0 head) are edited in place as
  * by pm_fuse; pruned (H x W), xyz (H*W x 3 floats, world frame), bgr_out

@@ -46,6 +46,44 @@ __global__ void fp32_probe_kernel(float *out, int iters, float a, float b) {
     if (s == 1.2345f) out[0] = s;  // keeps the chains alive
 }
 
+// Special-function-unit probe: 8 independent chains of x <- 2^-x per thread
+// (ex2.approx: one MUFU instruction, the unit whose reciprocal, reciprocal
+// square root and exponential the cost kernel issues; the negation folds
+// into the operand).  The chains converge to a fixed point near 0.64 and
+// cannot be simplified away.
+__global__ void sfu_probe_kernel(float *out, int iters) {
+    float x[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) x[c] = 0.5f + 1e-3f * (float)threadIdx.x + 0.1f * (float)c;
+    for (int k = 0; k < iters; ++k) {
+#pragma unroll
+        for (int u = 0; u < 16; ++u)
+#pragma unroll
+            for (int c = 0; c < 8; ++c) asm volatile("ex2.approx.ftz.f32 %0, %1;" : "=f"(x[c]) : "f"(-x[c]));
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) s += x[c];
+    if (s == 1.2345f) out[0] = s;
+}
+
+// Texture probe: independent bilinear fetches (8 per step) from a small u8
+// texture that stays in L1, at coordinates that move by a non-integer step so
+// every fetch filters four texels, as the cost kernel's samples do.
+__global__ void tex_probe_kernel(cudaTextureObject_t tex, float *out, int iters) {
+    const float u0 = 0.37f * (float)(threadIdx.x & 63) + 0.5f, v0 = 0.61f * (float)(threadIdx.x >> 6) + 0.5f;
+    float s[8] = {};
+    for (int k = 0; k < iters; ++k) {
+        const float du = 0.013f * (float)(k & 255);
+#pragma unroll
+        for (int c = 0; c < 8; ++c) s[c] += tex2D<float>(tex, u0 + du + 3.3f * c, v0 + 1.7f * c);
+    }
+    float t = 0.f;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) t += s[c];
+    if (t == 1.2345f) out[0] = t;
+}
+
 }  // namespace
 
 namespace {
@@ -124,12 +162,7 @@ bool finite_pose(const double *R, const double *t) {
 
 // X_k = M X_0 + c with M = R_k R_0^T, c = t_k - M t_0 (FP64, then rounded)
 void compose(const double *R0, const double *t0, const double *Rk, const double *tk, float *M, float *c) {
-    double Md[9];
-    for (int a = 0; a < 3; ++a)
-        for (int b = 0; b < 3; ++b)
-            Md[3 * a + b] = Rk[3 * a] * R0[3 * b] + Rk[3 * a + 1] * R0[3 * b + 1] + Rk[3 * a + 2] * R0[3 * b + 2];
-    for (int a = 0; a < 9; ++a) M[a] = (float)Md[a];
-    for (int a = 0; a < 3; ++a) c[a] = (float)(tk[a] - (Md[3 * a] * t0[0] + Md[3 * a + 1] * t0[1] + Md[3 * a + 2] * t0[2]));
+    pm::compose_pose(R0, t0, Rk, tk, M, c);
 }
 
 int validate_params(pm_ctx *ctx, const pm_params *p) {
@@ -760,6 +793,82 @@ int pm_probe_fp32_peak(pm_ctx *ctx, double *tflops) {
     return PM_OK;
 }
 
+// Time `launch` (one launch on the context's stream) four times and return
+// the best rate of `ops` operations per launch, in ops/s, over the last three.
+extern "C++" template <class F>
+int best_rate(pm_ctx *ctx, double ops, F launch, double *rate) {
+    cudaEvent_t e0, e1;
+    PM_CUDA(ctx, cudaEventCreate(&e0));
+    PM_CUDA(ctx, cudaEventCreate(&e1));
+    double best = 0.0;
+    for (int rep = 0; rep < 4; ++rep) {
+        PM_CUDA(ctx, cudaEventRecord(e0, ctx->stream));
+        launch();
+        PM_CUDA(ctx, cudaGetLastError());
+        PM_CUDA(ctx, cudaEventRecord(e1, ctx->stream));
+        PM_CUDA(ctx, cudaEventSynchronize(e1));
+        float ms = 0.f;
+        PM_CUDA(ctx, cudaEventElapsedTime(&ms, e0, e1));
+        if (rep > 0) best = std::max(best, ops / (ms * 1e-3));
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *rate = best;
+    return PM_OK;
+}
+
+int pm_probe_sfu_peak(pm_ctx *ctx, double *gops) {
+    if (!ctx || !gops) return fail(ctx, PM_EINVAL, "NULL argument");
+    PM_CUDA(ctx, cudaSetDevice(ctx->device));
+    int sms = 0;
+    PM_CUDA(ctx, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+    int rc = ensure_scratch(ctx, 256);
+    if (rc) return rc;
+    const int iters = 512, threads = 256, blocks = sms * 8;
+    double r = 0.0;
+    rc = best_rate(ctx, 8.0 * 16 * iters * threads * blocks, [&] {
+        sfu_probe_kernel<<<blocks, threads, 0, ctx->stream>>>((float *)ctx->scratch, iters);
+    }, &r);
+    *gops = r / 1e9;
+    return rc;
+}
+
+int pm_probe_tex_peak(pm_ctx *ctx, double *gfetches) {
+    if (!ctx || !gfetches) return fail(ctx, PM_EINVAL, "NULL argument");
+    PM_CUDA(ctx, cudaSetDevice(ctx->device));
+    int sms = 0, align = 0;
+    PM_CUDA(ctx, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+    PM_CUDA(ctx, cudaDeviceGetAttribute(&align, cudaDevAttrTexturePitchAlignment, ctx->device));
+    const int TW = 128, TH = 128;
+    const size_t pitch = ((size_t)TW + std::max(align, 32) - 1) / std::max(align, 32) * std::max(align, 32);
+    int rc = ensure_scratch(ctx, 512 + pitch * TH);
+    if (rc) return rc;
+    uint8_t *img = (uint8_t *)ctx->scratch + 512;  // the scratch block is 256-byte aligned
+    PM_CUDA(ctx, cudaMemsetAsync(img, 0x5A, pitch * TH, ctx->stream));
+    cudaResourceDesc res{};
+    res.resType = cudaResourceTypePitch2D;
+    res.res.pitch2D.devPtr = img;
+    res.res.pitch2D.desc = cudaCreateChannelDesc<uint8_t>();
+    res.res.pitch2D.width = TW;
+    res.res.pitch2D.height = TH;
+    res.res.pitch2D.pitchInBytes = pitch;
+    cudaTextureDesc td{};
+    td.addressMode[0] = cudaAddressModeClamp;
+    td.addressMode[1] = cudaAddressModeClamp;
+    td.filterMode = cudaFilterModeLinear;
+    td.readMode = cudaReadModeNormalizedFloat;
+    cudaTextureObject_t tex = 0;
+    PM_CUDA(ctx, cudaCreateTextureObject(&tex, &res, &td, nullptr));
+    const int iters = 256, threads = 256, blocks = sms * 8;
+    double r = 0.0;
+    rc = best_rate(ctx, 8.0 * iters * threads * blocks, [&] {
+        tex_probe_kernel<<<blocks, threads, 0, ctx->stream>>>(tex, (float *)ctx->scratch, iters);
+    }, &r);
+    cudaDestroyTextureObject(tex);
+    *gfetches = r / 1e9;
+    return rc;
+}
+
 size_t pm_request_bytes(int W, int H, int S, int fmt) {
     const size_t N = (size_t)W * H, NQ = (size_t)(W + 1) * (H + 1);
     const size_t qb = fmt == PM_IMAGE_F16 ? 8 : 4;
@@ -1289,134 +1398,175 @@ int pm_score_hypotheses(pm_request *r, int n, const int32_t *ij, const float *pl
     return PM_OK;
 }
 
-int pm_filter_consistency(pm_ctx *ctx, int W, int H, int n, const float *const *depths, const double *R,
-                          const double *t, int center, float thr, int min_consistent, float reproj_px, float *out) {
+// Arguments shared by the host- and device-buffer filter calls.
+static int filter_check(pm_ctx *ctx, int W, int H, int n, const float *const *depths, const double *R,
+                        const double *t, int center, float thr, const float *out) {
     if (!ctx || !depths || !R || !t || !out) return fail(ctx, PM_EINVAL, "NULL argument");
     if (W < 2 || H < 2 || n < 1 || n > pm::kMaxFilterViews || center < 0 || center >= n)
         return fail(ctx, PM_EINVAL, "bad sizes (W=%d H=%d n=%d center=%d)", W, H, n, center);
     for (int k = 0; k < n; ++k)
         if (!depths[k] || !finite_pose(R + 9 * k, t + 3 * k)) return fail(ctx, PM_EINVAL, "view %d invalid", k);
     if (!(thr > 0.0f)) return fail(ctx, PM_EINVAL, "same_depth_threshold must be > 0");
-    PM_CUDA(ctx, cudaSetDevice(ctx->device));
+    return PM_OK;
+}
+
+// Enqueue the filter on device maps (depths in caller order) on st.
+static int enqueue_filter(pm_ctx *ctx, int W, int H, int n, const float *const *depths, const double *R,
+                          const double *t, int center, float thr, int min_consistent, float reproj_px, float *out,
+                          cudaStream_t st) {
     Trig tr;
     int rc = get_trig(ctx, W, H, &tr);
     if (rc) return rc;
-    const size_t N = (size_t)W * H;
-    rc = ensure_scratch(ctx, (size_t)(n + 1) * align256(N * 4) + 256);
-    if (rc) return rc;
-    char *base = (char *)ctx->scratch;
-    std::vector<const float *> dptr(n);
-    // view order on the device: centre first, then the others in order
-    std::vector<int> order;
-    order.push_back(center);
-    for (int k = 0; k < n; ++k)
-        if (k != center) order.push_back(k);
-    for (int s = 0; s < n; ++s) {
-        float *d = (float *)(base + (size_t)s * align256(N * 4));
-        PM_CUDA(ctx, cudaMemcpyAsync(d, depths[order[s]], N * 4, cudaMemcpyHostToDevice, ctx->stream));
-        dptr[s] = d;
-    }
-    float *dout = (float *)(base + (size_t)n * align256(N * 4));
-    const float **dlist = nullptr;
-    PM_CUDA(ctx, cudaMallocAsync((void **)&dlist, sizeof(float *) * n, ctx->stream));
-    PM_CUDA(ctx, cudaMemcpyAsync(dlist, dptr.data(), sizeof(float *) * n, cudaMemcpyHostToDevice, ctx->stream));
     pm::CleanArgs a{};
-    a.depths = dlist;
-    a.n = n;
+    int order[pm::kMaxFilterViews];
+    pm::clean_set_poses(a, n, R, t, center, order);
+    for (int s = 0; s < n; ++s) a.depths[s] = depths[order[s]];
     a.W = W;
     a.H = H;
-    const double *R0 = R + 9 * center, *t0 = t + 3 * center;
-    for (int s = 1; s < n; ++s) {
-        const int k = order[s];
-        compose(R0, t0, R + 9 * k, t + 3 * k, a.M[s], a.c[s]);
-        compose(R + 9 * k, t + 3 * k, R0, t0, a.Minv[s], a.cinv[s]);
-    }
     a.row_trig = tr.row;
     a.col_trig = tr.col;
     a.thr = thr;
     a.min_consistent = min_consistent;
     a.reproj_px = reproj_px;
-    a.out = dout;
-    pm::launch_clean(ctx->stream, a);
+    a.out = out;
+    pm::launch_clean(st, a);
     ctx->launches++;
     PM_CUDA(ctx, cudaGetLastError());
+    return PM_OK;
+}
+
+int pm_filter_consistency(pm_ctx *ctx, int W, int H, int n, const float *const *depths, const double *R,
+                          const double *t, int center, float thr, int min_consistent, float reproj_px, float *out) {
+    int rc = filter_check(ctx, W, H, n, depths, R, t, center, thr, out);
+    if (rc) return rc;
+    PM_CUDA(ctx, cudaSetDevice(ctx->device));
+    const size_t N = (size_t)W * H;
+    rc = ensure_scratch(ctx, (size_t)(n + 1) * align256(N * 4));
+    if (rc) return rc;
+    char *base = (char *)ctx->scratch;
+    const float *dptr[pm::kMaxFilterViews];
+    for (int k = 0; k < n; ++k) {
+        float *d = (float *)(base + (size_t)k * align256(N * 4));
+        PM_CUDA(ctx, cudaMemcpyAsync(d, depths[k], N * 4, cudaMemcpyHostToDevice, ctx->stream));
+        dptr[k] = d;
+    }
+    float *dout = (float *)(base + (size_t)n * align256(N * 4));
+    rc = enqueue_filter(ctx, W, H, n, dptr, R, t, center, thr, min_consistent, reproj_px, dout, ctx->stream);
+    if (rc) return rc;
     PM_CUDA(ctx, cudaMemcpyAsync(out, dout, N * 4, cudaMemcpyDeviceToHost, ctx->stream));
-    PM_CUDA(ctx, cudaFreeAsync(dlist, ctx->stream));
     PM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return PM_OK;
 }
 
-int pm_fuse(pm_ctx *ctx, int W, int H, int n, float *const *depths, const double *R, const double *t,
-            const uint8_t *bgr, float thr, float *pruned, pm_points *out) {
-    if (!ctx || !depths || !R || !t || !pruned || !out) return fail(ctx, PM_EINVAL, "NULL argument");
+int pm_filter_consistency_device(pm_ctx *ctx, int W, int H, int n, const float *const *depths, const double *R,
+                                 const double *t, int center, float thr, int min_consistent, float reproj_px,
+                                 float *out, void *stream) {
+    int rc = filter_check(ctx, W, H, n, depths, R, t, center, thr, out);
+    if (rc) return rc;
+    PM_CUDA(ctx, cudaSetDevice(ctx->device));
+    return enqueue_filter(ctx, W, H, n, depths, R, t, center, thr, min_consistent, reproj_px, out,
+                          stream ? (cudaStream_t)stream : ctx->stream);
+}
+
+static int fuse_check(pm_ctx *ctx, int W, int H, int n, float *const *depths, const double *R, const double *t,
+                      float thr, const void *pruned) {
+    if (!ctx || !depths || !R || !t || !pruned) return fail(ctx, PM_EINVAL, "NULL argument");
     if (W < 2 || H < 2 || n < 1 || n > pm::kMaxFilterViews) return fail(ctx, PM_EINVAL, "bad sizes");
     for (int k = 0; k < n; ++k)
         if (!depths[k] || !finite_pose(R + 9 * k, t + 3 * k)) return fail(ctx, PM_EINVAL, "view %d invalid", k);
-    PM_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (!(thr > 0.0f)) return fail(ctx, PM_EINVAL, "same_depth_threshold must be > 0");
+    return PM_OK;
+}
+
+// Enqueue the fusion on device maps with a caller workspace on st.
+static int enqueue_fuse(pm_ctx *ctx, int W, int H, int n, float *const *depths, const double *R, const double *t,
+                        const uint8_t *bgr, float thr, float *pruned, float *xyz, uint8_t *bgr_out, int32_t *ij,
+                        unsigned *count, void *ws, cudaStream_t st) {
     Trig tr;
     int rc = get_trig(ctx, W, H, &tr);
     if (rc) return rc;
+    pm::FuseArgs a{};
+    a.W = W;
+    a.H = H;
+    for (int k = 0; k < n; ++k) a.depths[k] = depths[k];
+    pm::fuse_set_poses(a, n, R, t);
+    pm::fuse_bind_workspace(a, ws);
+    a.row_trig = tr.row;
+    a.col_trig = tr.col;
+    a.thr = thr;
+    a.pruned = pruned;
+    a.bgr = bgr;
+    a.xyz = xyz;
+    a.bgr_out = bgr ? bgr_out : nullptr;
+    a.ij_out = ij;
+    a.count = count;
+    const cudaError_t e = pm::launch_fuse(st, a);
+    ctx->launches += 1 + 2 * (uint64_t)(n - 1) + 3;
+    if (e != cudaSuccess) return fail(ctx, PM_ECUDA, "fusion: %s", cudaGetErrorString(e));
+    return PM_OK;
+}
+
+size_t pm_fuse_workspace_bytes(int W, int H) {
+    if (W < 2 || H < 2) return 0;
+    return pm::fuse_workspace_bytes(W, H);
+}
+
+int pm_fuse_device(pm_ctx *ctx, int W, int H, int n, float *const *depths, const double *R, const double *t,
+                   const uint8_t *bgr, float thr, float *pruned, float *xyz, uint8_t *bgr_out, int32_t *ij,
+                   unsigned *count, void *workspace, size_t workspace_bytes, void *stream) {
+    int rc = fuse_check(ctx, W, H, n, depths, R, t, thr, pruned);
+    if (rc) return rc;
+    if (!xyz || !count || !workspace) return fail(ctx, PM_EINVAL, "NULL argument");
+    if (workspace_bytes < pm::fuse_workspace_bytes(W, H) || ((uintptr_t)workspace & 255))
+        return fail(ctx, PM_EINVAL, "workspace must be 256-byte aligned and hold pm_fuse_workspace_bytes");
+    PM_CUDA(ctx, cudaSetDevice(ctx->device));
+    return enqueue_fuse(ctx, W, H, n, depths, R, t, bgr, thr, pruned, xyz, bgr_out, ij, count, workspace,
+                        stream ? (cudaStream_t)stream : ctx->stream);
+}
+
+int pm_fuse(pm_ctx *ctx, int W, int H, int n, float *const *depths, const double *R, const double *t,
+            const uint8_t *bgr, float thr, float *pruned, pm_points *out) {
+    int rc = fuse_check(ctx, W, H, n, depths, R, t, thr, pruned);
+    if (rc) return rc;
+    if (!out) return fail(ctx, PM_EINVAL, "NULL argument");
+    PM_CUDA(ctx, cudaSetDevice(ctx->device));
     const size_t N = (size_t)W * H;
-    const int nb = (int)((N + 1023) / 1024);
-    const size_t need = (size_t)n * align256(N * 4) + align256(N) + align256(N * 4) + align256(N) + align256(N * 4) +
-                        align256(N * 4) + align256((size_t)(nb + 1) * 4) + align256(N * 3) + align256(N * 12) +
-                        align256(N * 3) + align256(N * 8) + 256;
+    const size_t need = (size_t)n * align256(N * 4) + align256(pm::fuse_workspace_bytes(W, H)) + align256(N * 4) +
+                        align256(N * 3) + align256(N * 12) + align256(N * 3) + align256(N * 8) + 256;
     rc = ensure_scratch(ctx, need);
     if (rc) return rc;
     char *p = (char *)ctx->scratch;
     auto take = [&](size_t b) { void *q = p; p += align256(b); return q; };
-    std::vector<float *> dptr(n);
+    float *dptr[pm::kMaxFilterViews];
     for (int k = 0; k < n; ++k) {
         dptr[k] = (float *)take(N * 4);
         PM_CUDA(ctx, cudaMemcpyAsync(dptr[k], depths[k], N * 4, cudaMemcpyHostToDevice, ctx->stream));
     }
-    pm::FuseArgs a{};
-    a.alive = (uint8_t *)take(N);
-    a.target = (int *)take(N * 4);
-    a.cls = (int8_t *)take(N);
-    a.first = (unsigned *)take(N * 4);
-    a.pruned = (float *)take(N * 4);
-    a.block_counts = (unsigned *)take((size_t)(nb + 1) * 4);
+    void *ws = take(pm::fuse_workspace_bytes(W, H));
+    float *dpruned = (float *)take(N * 4);
     uint8_t *dbgr = (uint8_t *)take(N * 3);
-    a.xyz = (float *)take(N * 12);
-    a.bgr_out = (uint8_t *)take(N * 3);
-    a.ij_out = (int *)take(N * 8);
-    a.count = (unsigned *)take(4);
+    float *dxyz = (float *)take(N * 12);
+    uint8_t *dbgr_out = (uint8_t *)take(N * 3);
+    int32_t *dij = (int32_t *)take(N * 8);
+    unsigned *dcount = (unsigned *)take(4);
     if (bgr) PM_CUDA(ctx, cudaMemcpyAsync(dbgr, bgr, N * 3, cudaMemcpyHostToDevice, ctx->stream));
-    a.bgr = bgr ? dbgr : nullptr;
-    float **dlist = nullptr;
-    PM_CUDA(ctx, cudaMallocAsync((void **)&dlist, sizeof(float *) * n, ctx->stream));
-    PM_CUDA(ctx, cudaMemcpyAsync(dlist, dptr.data(), sizeof(float *) * n, cudaMemcpyHostToDevice, ctx->stream));
-    a.depths = dlist;
-    a.n = n;
-    a.W = W;
-    a.H = H;
-    for (int k = 1; k < n; ++k) compose(R, t, R + 9 * k, t + 3 * k, a.M[k], a.c[k]);
-    for (int r0 = 0; r0 < 3; ++r0) {
-        for (int c0 = 0; c0 < 3; ++c0) a.Rinv[3 * r0 + c0] = (float)R[3 * c0 + r0];
-        a.tw[r0] = (float)(-(R[r0] * t[0] + R[3 + r0] * t[1] + R[6 + r0] * t[2]));
-    }
-    a.row_trig = tr.row;
-    a.col_trig = tr.col;
-    a.thr = thr;
-    pm::launch_fuse(ctx->stream, a);
-    ctx->launches += 1 + 2 * (uint64_t)(n - 1) + 3;
-    PM_CUDA(ctx, cudaGetLastError());
+    rc = enqueue_fuse(ctx, W, H, n, dptr, R, t, bgr ? dbgr : nullptr, thr, dpruned, dxyz, dbgr_out, dij, dcount, ws,
+                      ctx->stream);
+    if (rc) return rc;
     unsigned count = 0;
-    PM_CUDA(ctx, cudaMemcpyAsync(&count, a.count, 4, cudaMemcpyDeviceToHost, ctx->stream));
-    PM_CUDA(ctx, cudaMemcpyAsync(pruned, a.pruned, N * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    PM_CUDA(ctx, cudaMemcpyAsync(&count, dcount, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    PM_CUDA(ctx, cudaMemcpyAsync(pruned, dpruned, N * 4, cudaMemcpyDeviceToHost, ctx->stream));
     for (int k = 1; k < n; ++k)
         PM_CUDA(ctx, cudaMemcpyAsync(depths[k], dptr[k], N * 4, cudaMemcpyDeviceToHost, ctx->stream));
-    PM_CUDA(ctx, cudaFreeAsync(dlist, ctx->stream));
     PM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     const int m = (int)std::min<unsigned>(count, out->capacity > 0 ? (unsigned)out->capacity : 0u);
     if (m > 0) {
         std::vector<float> xyz((size_t)m * 3);
-        PM_CUDA(ctx, cudaMemcpy(xyz.data(), a.xyz, (size_t)m * 12, cudaMemcpyDeviceToHost));
+        PM_CUDA(ctx, cudaMemcpy(xyz.data(), dxyz, (size_t)m * 12, cudaMemcpyDeviceToHost));
         if (out->xyz)
             for (size_t q = 0; q < (size_t)m * 3; ++q) out->xyz[q] = xyz[q];
-        if (out->bgr && bgr) PM_CUDA(ctx, cudaMemcpy(out->bgr, a.bgr_out, (size_t)m * 3, cudaMemcpyDeviceToHost));
-        if (out->ij) PM_CUDA(ctx, cudaMemcpy(out->ij, a.ij_out, (size_t)m * 8, cudaMemcpyDeviceToHost));
+        if (out->bgr && bgr) PM_CUDA(ctx, cudaMemcpy(out->bgr, dbgr_out, (size_t)m * 3, cudaMemcpyDeviceToHost));
+        if (out->ij) PM_CUDA(ctx, cudaMemcpy(out->ij, dij, (size_t)m * 8, cudaMemcpyDeviceToHost));
     }
     out->count = (int)count;
     if ((int)count > out->capacity)

@@ -21,7 +21,8 @@ namespace {
 
 constexpr size_t kMaxPix = PM_FUSE_NOALLOC_MAX_PIXELS;
 constexpr int kMaxW = PM_FUSE_NOALLOC_MAX_WIDTH, kMaxH = PM_FUSE_NOALLOC_MAX_HEIGHT;
-constexpr size_t kBlocks = (kMaxPix + 1023) / 1024 + 1;
+// compaction blocks of the largest image, plus the scan's total slot
+constexpr size_t kBlocks = (kMaxPix + pm::kCompactBlock - 1) / pm::kCompactBlock + 1;
 
 // All working memory of one fusion, shared by every call on a device.
 struct FuseScratch {
@@ -30,8 +31,6 @@ struct FuseScratch {
     int target[kMaxPix];
     unsigned first[kMaxPix];
     unsigned block_counts[kBlocks];
-    unsigned count;
-    float *depths[pm::kMaxFilterViews];
     float2 row_trig[kMaxH];
     float2 col_trig[kMaxW];
 };
@@ -40,7 +39,10 @@ static __device__ __align__(256) FuseScratch g_fuse_scratch;
 
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
-FuseScratch *g_scratch_dev[kMaxDevices] = {};  // device address per device, from cudaGetSymbolAddress
+// per device: the device address of g_fuse_scratch (from cudaGetSymbolAddress)
+// and the image size whose bearing tables it holds
+FuseScratch *g_scratch_dev[kMaxDevices] = {};
+int g_trig_w[kMaxDevices] = {}, g_trig_h[kMaxDevices] = {};
 float2 g_row_host[kMaxH], g_col_host[kMaxW];   // host staging of the bearing tables (guarded by g_mu)
 
 }  // namespace
@@ -58,6 +60,8 @@ extern "C" int pm_fuse_noalloc(int W, int H, int n, float *const *depths, const 
         for (int a = 0; a < 3; ++a)
             if (!std::isfinite(t[3 * k + a])) return PM_EINVAL;
     }
+    // a launch error left pending by earlier work on this thread is not this call's
+    cudaGetLastError();
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return PM_ECUDA;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
@@ -74,41 +78,32 @@ extern "C" int pm_fuse_noalloc(int W, int H, int n, float *const *depths, const 
     }
     FuseScratch *s = g_scratch_dev[dev];
 
-    // bearing tables and the depth-map pointer table (same FP64 rounding as pm_fuse)
-    for (int i = 0; i < H; ++i) {
-        const double lat = -M_PI * ((double)i / H - 0.5);
-        g_row_host[i] = make_float2((float)std::cos(lat), (float)std::sin(lat));
-    }
-    for (int j = 0; j < W; ++j) {
-        const double lon = 2.0 * M_PI * ((double)j / W - 0.5);
-        g_col_host[j] = make_float2((float)std::sin(lon), (float)std::cos(lon));
-    }
-    if (cudaMemcpyAsync(s->row_trig, g_row_host, sizeof(float2) * H, cudaMemcpyHostToDevice, st) != cudaSuccess ||
-        cudaMemcpyAsync(s->col_trig, g_col_host, sizeof(float2) * W, cudaMemcpyHostToDevice, st) != cudaSuccess ||
-        cudaMemcpyAsync(s->depths, depths, sizeof(float *) * n, cudaMemcpyHostToDevice, st) != cudaSuccess) {
-        cudaGetLastError();
-        return PM_ECUDA;
+    // bearing tables (same FP64 rounding as pm_fuse), copied from host memory
+    // on the first call of each image size on this device only
+    if (g_trig_w[dev] != W || g_trig_h[dev] != H) {
+        for (int i = 0; i < H; ++i) {
+            const double lat = -M_PI * ((double)i / H - 0.5);
+            g_row_host[i] = make_float2((float)std::cos(lat), (float)std::sin(lat));
+        }
+        for (int j = 0; j < W; ++j) {
+            const double lon = 2.0 * M_PI * ((double)j / W - 0.5);
+            g_col_host[j] = make_float2((float)std::sin(lon), (float)std::cos(lon));
+        }
+        // pageable sources: staged before the calls return, so the host tables may change afterwards
+        if (cudaMemcpyAsync(s->row_trig, g_row_host, sizeof(float2) * H, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+            cudaMemcpyAsync(s->col_trig, g_col_host, sizeof(float2) * W, cudaMemcpyHostToDevice, st) != cudaSuccess) {
+            cudaGetLastError();
+            g_trig_w[dev] = g_trig_h[dev] = 0;
+            return PM_ECUDA;
+        }
+        g_trig_w[dev] = W;
+        g_trig_h[dev] = H;
     }
     pm::FuseArgs a{};
-    a.depths = s->depths;
-    a.n = n;
     a.W = W;
     a.H = H;
-    for (int k = 1; k < n; ++k) {
-        // head camera -> view k, composed in FP64 (as pm_fuse)
-        double Md[9];
-        for (int r0 = 0; r0 < 3; ++r0)
-            for (int c0 = 0; c0 < 3; ++c0)
-                Md[3 * r0 + c0] = R[9 * k + 3 * r0] * R[3 * c0] + R[9 * k + 3 * r0 + 1] * R[3 * c0 + 1] +
-                                  R[9 * k + 3 * r0 + 2] * R[3 * c0 + 2];
-        for (int q = 0; q < 9; ++q) a.M[k][q] = (float)Md[q];
-        for (int r0 = 0; r0 < 3; ++r0)
-            a.c[k][r0] = (float)(t[3 * k + r0] - (Md[3 * r0] * t[0] + Md[3 * r0 + 1] * t[1] + Md[3 * r0 + 2] * t[2]));
-    }
-    for (int r0 = 0; r0 < 3; ++r0) {
-        for (int c0 = 0; c0 < 3; ++c0) a.Rinv[3 * r0 + c0] = (float)R[3 * c0 + r0];
-        a.tw[r0] = (float)(-(R[r0] * t[0] + R[3 + r0] * t[1] + R[6 + r0] * t[2]));
-    }
+    for (int k = 0; k < n; ++k) a.depths[k] = depths[k];  // by value, in the kernel parameters
+    pm::fuse_set_poses(a, n, R, t);                      // FP64-composed, as pm_fuse
     a.row_trig = s->row_trig;
     a.col_trig = s->col_trig;
     a.thr = thr;
@@ -127,7 +122,5 @@ extern "C" int pm_fuse_noalloc(int W, int H, int n, float *const *depths, const 
     // (alive/pruned by the init kernel, cls/target by classify, first by the
     // memset, block_counts by the count kernel), so nothing from the previous
     // call leaks in
-    pm::launch_fuse(st, a);
-    if (cudaGetLastError() != cudaSuccess) return PM_ECUDA;
-    return PM_OK;
+    return pm::launch_fuse(st, a) == cudaSuccess ? PM_OK : PM_ECUDA;
 }

@@ -88,24 +88,40 @@ void launch_export(cudaStream_t st, const float4 *plane, const float *score, con
                    int W, int H, int raw, float *depth, float *score_out, float *plane3, float *normal3,
                    int32_t *best32);
 
+// Depth maps a consistency filter or a fusion call takes at most.
+constexpr int kMaxFilterViews = PM_MAX_SOURCES + 6;
+
+// Camera k relative to camera 0 from world->camera poses, composed in FP64
+// and rounded to float: X_k = M X_0 + c with M = R_k R_0^T, c = t_k - M t_0.
+inline void compose_pose(const double *R0, const double *t0, const double *Rk, const double *tk, float *M, float *c) {
+    double Md[9];
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b)
+            Md[3 * a + b] = Rk[3 * a] * R0[3 * b] + Rk[3 * a + 1] * R0[3 * b + 1] + Rk[3 * a + 2] * R0[3 * b + 2];
+    for (int a = 0; a < 9; ++a) M[a] = (float)Md[a];
+    for (int a = 0; a < 3; ++a) c[a] = (float)(tk[a] - (Md[3 * a] * t0[0] + Md[3 * a + 1] * t0[1] + Md[3 * a + 2] * t0[2]));
+}
+
 struct CleanArgs {
-    const float *const *depths;  // device array of n device pointers; view 0 = centre
+    const float *depths[kMaxFilterViews];  // device pointers, view 0 = centre (passed by value)
     int n, W, H;
-    float M[PM_MAX_SOURCES + 6][9];  // centre camera -> view k (k >= 1)
-    float c[PM_MAX_SOURCES + 6][3];
-    float Minv[PM_MAX_SOURCES + 6][9];  // view k -> centre camera (round trip)
-    float cinv[PM_MAX_SOURCES + 6][3];
+    float M[kMaxFilterViews][9];  // centre camera -> view k (k >= 1)
+    float c[kMaxFilterViews][3];
+    float Minv[kMaxFilterViews][9];  // view k -> centre camera (round trip)
+    float cinv[kMaxFilterViews][3];
     const float2 *row_trig, *col_trig;
     float thr;
     int min_consistent;
     float reproj_px;
     float *out;
 };
-constexpr int kMaxFilterViews = PM_MAX_SOURCES + 6;
+// Poses of a filter call: view `center` of R/t (world->camera) becomes view 0,
+// the others follow in order (order[s] = original index of view s).
+void clean_set_poses(CleanArgs &a, int n, const double *R, const double *t, int center, int *order);
 void launch_clean(cudaStream_t st, const CleanArgs &a);
 
 struct FuseArgs {
-    float *const *depths;  // device array of n device pointers; view 0 = head
+    float *depths[kMaxFilterViews];  // device pointers, view 0 = head (passed by value)
     int n, W, H;
     float M[kMaxFilterViews][9];  // head camera -> view k
     float c[kMaxFilterViews][3];
@@ -125,6 +141,17 @@ struct FuseArgs {
     int *ij_out;                   // out
     unsigned *count;               // out (device)
 };
-void launch_fuse(cudaStream_t st, const FuseArgs &a);
+// Pixels per block of the fusion's output compaction (count, scan, scatter).
+constexpr int kCompactBlock = 1024;
+// Working memory of one fusion (alive, target, cls, first, block counts) as one
+// device block of fuse_workspace_bytes(W, H) bytes, 256-byte aligned.
+size_t fuse_workspace_bytes(int W, int H);
+void fuse_bind_workspace(FuseArgs &a, void *ws);
+// Poses of a fusion (R/t world->camera, view 0 = head): head camera -> view k
+// and head camera -> world.
+void fuse_set_poses(FuseArgs &a, int n, const double *R, const double *t);
+// Every scratch entry a launch reads is written earlier in the same call, so
+// nothing from a previous call on the same workspace leaks in.
+cudaError_t launch_fuse(cudaStream_t st, const FuseArgs &a);
 
 }  // namespace pm

@@ -274,8 +274,6 @@ __global__ void fuse_resolve_kernel(const __grid_constant__ FuseArgs a, int k) {
     }
 }
 
-constexpr int kCompactBlock = 1024;
-
 __global__ void compact_count_kernel(const uint8_t *alive, size_t N, unsigned *counts) {
     const size_t i = (size_t)blockIdx.x * kCompactBlock + threadIdx.x;
     const int keep = (i < N) ? alive[i] : 0;
@@ -367,24 +365,69 @@ void launch_export(cudaStream_t st, const float4 *plane, const float *score, con
                                    score_out, plane3, normal3, best32);
 }
 
+void clean_set_poses(CleanArgs &a, int n, const double *R, const double *t, int center, int *order) {
+    order[0] = center;
+    for (int k = 0, s = 1; k < n; ++k)
+        if (k != center) order[s++] = k;
+    const double *R0 = R + 9 * center, *t0 = t + 3 * center;
+    for (int s = 1; s < n; ++s) {
+        const int k = order[s];
+        compose_pose(R0, t0, R + 9 * k, t + 3 * k, a.M[s], a.c[s]);
+        compose_pose(R + 9 * k, t + 3 * k, R0, t0, a.Minv[s], a.cinv[s]);
+    }
+    a.n = n;
+}
+
 void launch_clean(cudaStream_t st, const CleanArgs &a) {
     dim3 b(32, 8), g((a.W + 31) / 32, (a.H + 7) / 8);
     clean_kernel<<<g, b, 0, st>>>(a);
 }
 
-void launch_fuse(cudaStream_t st, const FuseArgs &a) {
+namespace {
+inline size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
+inline int compact_blocks(int W, int H) { return (int)(((size_t)W * H + kCompactBlock - 1) / kCompactBlock); }
+}  // namespace
+
+size_t fuse_workspace_bytes(int W, int H) {
+    const size_t N = (size_t)W * H;
+    return al256(N) + al256(N * 4) + al256(N) + al256(N * 4) + al256((size_t)(compact_blocks(W, H) + 1) * 4);
+}
+
+void fuse_bind_workspace(FuseArgs &a, void *ws) {
+    const size_t N = (size_t)a.W * a.H;
+    char *p = static_cast<char *>(ws);
+    auto take = [&](size_t b) { char *q = p; p += al256(b); return q; };
+    a.alive = reinterpret_cast<uint8_t *>(take(N));
+    a.target = reinterpret_cast<int *>(take(N * 4));
+    a.cls = reinterpret_cast<int8_t *>(take(N));
+    a.first = reinterpret_cast<unsigned *>(take(N * 4));
+    a.block_counts = reinterpret_cast<unsigned *>(take((size_t)(compact_blocks(a.W, a.H) + 1) * 4));
+}
+
+void fuse_set_poses(FuseArgs &a, int n, const double *R, const double *t) {
+    for (int k = 1; k < n; ++k) compose_pose(R, t, R + 9 * k, t + 3 * k, a.M[k], a.c[k]);
+    for (int r0 = 0; r0 < 3; ++r0) {
+        for (int c0 = 0; c0 < 3; ++c0) a.Rinv[3 * r0 + c0] = (float)R[3 * c0 + r0];
+        a.tw[r0] = (float)(-(R[r0] * t[0] + R[3 + r0] * t[1] + R[6 + r0] * t[2]));
+    }
+    a.n = n;
+}
+
+cudaError_t launch_fuse(cudaStream_t st, const FuseArgs &a) {
     dim3 b(32, 8), g((a.W + 31) / 32, (a.H + 7) / 8);
     const size_t N = (size_t)a.W * a.H;
     fuse_init_kernel<<<g, b, 0, st>>>(a);
     for (int k = 1; k < a.n; ++k) {
-        cudaMemsetAsync(a.first, 0xFF, N * sizeof(unsigned), st);
+        const cudaError_t e = cudaMemsetAsync(a.first, 0xFF, N * sizeof(unsigned), st);
+        if (e != cudaSuccess) return e;
         fuse_classify_kernel<<<g, b, 0, st>>>(a, k);
         fuse_resolve_kernel<<<g, b, 0, st>>>(a, k);
     }
-    const int nb = (int)((N + kCompactBlock - 1) / kCompactBlock);
+    const int nb = compact_blocks(a.W, a.H);
     compact_count_kernel<<<nb, kCompactBlock, 0, st>>>(a.alive, N, a.block_counts);
     compact_scan_kernel<<<1, 1024, 0, st>>>(a.block_counts, nb, a.count);
     compact_scatter_kernel<<<nb, kCompactBlock, 0, st>>>(a);
+    return cudaGetLastError();
 }
 
 }  // namespace pm

@@ -38,6 +38,8 @@ EXPORTS = (
     "pm_request_run", "pm_request_read", "pm_request_read_async", "pm_request_synchronize", "pm_request_query",
     "pm_request_stream", "pm_request_depth_device",
     "pm_score_hypotheses", "pm_filter_consistency", "pm_fuse", "pm_fuse_noalloc",
+    "pm_filter_consistency_device", "pm_fuse_workspace_bytes", "pm_fuse_device", "pm_probe_sfu_peak",
+    "pm_probe_tex_peak",
     "pm_server_config_default", "pm_server_create", "pm_server_submit", "pm_server_wait", "pm_server_destroy",
 )
 
@@ -100,6 +102,8 @@ def lib():
     L.pm_stream.restype = _vp
     L.pm_stream.argtypes = [_vp]
     L.pm_probe_fp32_peak.argtypes = [_vp, C.POINTER(C.c_double)]
+    L.pm_probe_sfu_peak.argtypes = [_vp, C.POINTER(C.c_double)]
+    L.pm_probe_tex_peak.argtypes = [_vp, C.POINTER(C.c_double)]
     L.pm_densify.argtypes = [_vp, C.c_int, C.c_int, C.POINTER(View), C.c_int, C.POINTER(Params), C.POINTER(Maps)]
     L.pm_request_create.argtypes = [_vp, C.c_int, C.c_int, C.c_int, C.POINTER(Params), C.POINTER(_vp)]
     L.pm_request_destroy.argtypes = [_vp]
@@ -136,6 +140,12 @@ def lib():
     L.pm_fuse.argtypes = [_vp, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, C.c_float, _vp, C.POINTER(Points)]
     L.pm_fuse_noalloc.argtypes = [C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, C.c_float, _vp, _vp, _vp, _vp, _vp,
                                   _vp]
+    L.pm_filter_consistency_device.argtypes = [_vp, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, C.c_int, C.c_float,
+                                               C.c_int, C.c_float, _vp, _vp]
+    L.pm_fuse_workspace_bytes.restype = C.c_size_t
+    L.pm_fuse_workspace_bytes.argtypes = [C.c_int, C.c_int]
+    L.pm_fuse_device.argtypes = [_vp, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, C.c_float, _vp, _vp, _vp, _vp,
+                                 _vp, _vp, C.c_size_t, _vp]
     L.pm_batch_create.argtypes = [_vp, C.POINTER(_vp)]
     for f in ("pm_batch_clear", "pm_batch_run", "pm_batch_synchronize", "pm_batch_destroy"):
         getattr(L, f).argtypes = [_vp]
@@ -343,6 +353,18 @@ class Context:
         self.check(self._L.pm_probe_fp32_peak(self.h, C.byref(v)))
         return v.value
 
+    def probe_sfu_peak(self) -> float:
+        """Measured special-function (approximate reciprocal) throughput, Gop/s."""
+        v = C.c_double()
+        self.check(self._L.pm_probe_sfu_peak(self.h, C.byref(v)))
+        return v.value
+
+    def probe_tex_peak(self) -> float:
+        """Measured bilinear texture-fetch throughput (L1-resident u8), Gfetch/s."""
+        v = C.c_double()
+        self.check(self._L.pm_probe_tex_peak(self.h, C.byref(v)))
+        return v.value
+
     def last_error(self) -> str:
         return self._L.pm_last_error(self.h).decode()
 
@@ -391,6 +413,32 @@ class Context:
                                    thr, _ptr(pruned), C.byref(pts)))
         n = pts.count
         return pruned, xyz[:n], cols[:n], ij[:n], depths
+
+
+    def filter_consistency_device(self, depth_ptrs, W: int, H: int, R, t, center: int, thr: float, out_ptr: int,
+                                  min_consistent: int = 3, reproj_px: float = 0.0, stream: int = 0):
+        """pm_filter_consistency_device: device pointers in and out, enqueued on `stream` (0: the context's)."""
+        arr = (C.c_void_p * len(depth_ptrs))(*depth_ptrs)
+        R = np.ascontiguousarray(R, np.float64)
+        t = np.ascontiguousarray(t, np.float64)
+        self.check(self._L.pm_filter_consistency_device(self.h, W, H, len(depth_ptrs), C.cast(arr, C.c_void_p),
+                                                        _ptr(R), _ptr(t), center, thr, min_consistent, reproj_px,
+                                                        out_ptr, stream or None))
+
+    def fuse_device(self, depth_ptrs, W: int, H: int, R, t, thr: float, pruned_ptr: int, xyz_ptr: int, count_ptr: int,
+                    workspace_ptr: int, workspace_bytes: int, bgr_ptr: int = 0, bgr_out_ptr: int = 0, ij_ptr: int = 0,
+                    stream: int = 0):
+        """pm_fuse_device: device pointers in and out, enqueued on `stream` (0: the context's)."""
+        arr = (C.c_void_p * len(depth_ptrs))(*depth_ptrs)
+        R = np.ascontiguousarray(R, np.float64)
+        t = np.ascontiguousarray(t, np.float64)
+        self.check(self._L.pm_fuse_device(self.h, W, H, len(depth_ptrs), C.cast(arr, C.c_void_p), _ptr(R), _ptr(t),
+                                          bgr_ptr or None, thr, pruned_ptr, xyz_ptr, bgr_out_ptr or None,
+                                          ij_ptr or None, count_ptr, workspace_ptr, workspace_bytes, stream or None))
+
+
+def fuse_workspace_bytes(W: int, H: int) -> int:
+    return int(lib().pm_fuse_workspace_bytes(W, H))
 
 
 def _alloc_maps(H, W, want):
@@ -497,6 +545,11 @@ class Request:
     def stream_handle(self) -> int:
         """cudaStream_t of the request (for torch.cuda.ExternalStream)."""
         return int(self._L.pm_request_stream(self.h))
+
+    @property
+    def depth_device_ptr(self) -> int:
+        """Device address of the request's filtered depth map (H x W floats)."""
+        return int(self._L.pm_request_depth_device(self.h))
 
     def done(self) -> bool:
         rc = self._L.pm_request_query(self.h)

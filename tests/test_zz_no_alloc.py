@@ -70,6 +70,26 @@ def test_noalloc_fuse_matches_pm_fuse_twice_in_a_row(built):
     ctx.close()
 
 
+def test_noalloc_fuse_at_the_maximum_size(built):
+    """2048 x 1024 = PM_FUSE_NOALLOC_MAX_PIXELS: the compaction scan runs over
+    more than 1024 blocks and fills the array's last block-count slot."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    ctx = native.Context(0)
+    req, depths = _inputs(43, 2048, 1024, 3, 0.05)
+    bgr = req.views[0].rgb
+    p0, x0, c0, ij0, m0 = ctx.fuse(depths, req.R, req.t, bgr, 0.02)
+    p1, x1, c1, ij1, m1 = _run_noalloc(depths, req.R, req.t, bgr, 0.02)
+    assert np.array_equal(p0, p1)
+    assert len(x0) == len(x1) > 0
+    assert np.array_equal(ij0, ij1) and np.array_equal(c0, c1)
+    assert np.allclose(x0, x1.astype(np.float64), rtol=0, atol=1e-6)
+    for a, b in zip(m0, m1):
+        assert np.array_equal(a, b)
+    ctx.close()
+
+
 def test_noalloc_rejects_oversize_and_bad_arguments(built):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
