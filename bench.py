@@ -799,6 +799,21 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_profile_sweep():
+    """One densification of the 1920x960x6 keyframe (init scoring, 16
+    half-sweeps, post-filter) and nothing else: the case the sweep kernel's
+    ncu captures select launches from (tile_kernel launch 0 is the init
+    scoring, launch k the k-th half-sweep)."""
+    from patchmatch_gb300 import native, scene
+    req = scene.config_request(2, seed=0)
+    with native.Context(0) as ctx:
+        r = ctx.request(W, H, S, native.default_params(iterations=SWEEPS, combine=native.COMBINE_TOPK, top_k=TOP_K))
+        r.set_views([v.gray_u8 for v in req.views], req.R, req.t)
+        r.run()
+        r.synchronize()
+        r.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -815,8 +830,12 @@ def main():
     ap.add_argument("--served-rate", type=float, default=4.0, help="arrival rate of the capacity stream (Hz)")
     ap.add_argument("--served-seconds", type=float, default=30.0, help="length of the capacity stream (s)")
     ap.add_argument("--latency-seconds", type=float, default=20.0, help="length of the 10 Hz latency stream (s)")
+    ap.add_argument("--profile-sweep", action="store_true",
+                    help="densify one keyframe and exit (the case for ncu captures of the sweep kernel)")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.profile_sweep:
+        run_profile_sweep()
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)
