@@ -7,8 +7,8 @@
 // so the reference's densification thread (depthmap_computation_module.cc:
 // 364-414) and fusion thread (dense_pointcloud_module.cc:115-143) can drive
 // it unchanged apart from the matrix/image types.  OpenCV is not a dependency:
-// images are row-major byte buffers and poses are FP64 arrays; the
-// OpenCV adapter a maintainer adds is shown in INTEGRATION.md.
+// images are row-major byte buffers and poses are FP64 arrays; an adapter
+// from cv::Mat / cv::Matx33d wraps their data pointers without copies.
 //
 // Differences from the reference, all deliberate:
 //   - errors are reported by return values (the reference prints and goes on);

@@ -18,7 +18,10 @@ import subprocess
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REFERENCE_SRC = "/root/reference/src/openvslam/PatchMatchCuda.cu"
+# Where the reference project lies: PM_REFERENCE_ROOT, else its checkout in
+# the development container (absent on machines that only run the tests).
+REFERENCE_ROOT = os.environ.get("PM_REFERENCE_ROOT", "/root/reference")
+REFERENCE_SRC = os.path.join(REFERENCE_ROOT, "src", "openvslam", "PatchMatchCuda.cu")
 REF_DIR = os.path.join(HERE, "_ref")
 FATBIN = os.path.join(REF_DIR, "refpm_sm103a.fatbin")
 HARNESS_SRC = os.path.join(HERE, "ref_harness.cu")
