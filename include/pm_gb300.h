@@ -60,6 +60,11 @@ extern "C" {
 /* longitude seam handling of bilinear source samples */
 #define PM_SEAM_CLAMP 0    /* clamp at the image border (the reference's texture behaviour) */
 #define PM_SEAM_WRAP 1     /* wrap around in longitude (360-degree continuity) */
+#define PM_SEAM_ZERO 2     /* the reference host cost's border: a sample whose bilinear footprint leaves
+                              [0, W-1) x [0, H-1) reads 0 (LinearInterpolation, depthmap.cc:34-38);
+                              with PM_SAMPLER_EXACT and PM_COMBINE_MAX this is
+                              ComputePlaneImageScoreUnoptimized_equirect + ComputePlaneScore
+                              (depthmap.cc:1104-1157) for interior pixels */
 
 /* initialisation */
 #define PM_INIT_LOGUNIFORM_HEMI 0 /* log-uniform depth, unit normals on the camera-facing hemisphere */
@@ -261,6 +266,9 @@ void *pm_request_stream(const pm_request *req);
 /* Device pointer of the (filtered) depth map, H x W float, for chaining into
  * pm_filter_consistency_device / pm_fuse_device without a host round trip. */
 const float *pm_request_depth_device(const pm_request *req);
+/* The same for a retained result (its snapshot of the filtered depth); valid
+ * once the snapshot's request stream has passed pm_result_snapshot. */
+const float *pm_result_depth_device(const pm_result *res);
 
 /* Score n fixed plane hypotheses at pixels ij[2n] (row, col) against the
  * request's views: the cost kernel in isolation.  scores[n], best[n] and
@@ -353,6 +361,19 @@ typedef struct {
                                 densified at half resolution first (params.iterations sweeps) and
                                 then refined at full resolution (seeded_iterations sweeps) seeded
                                 from that result */
+    int dense_output;        /* 1: run the geometric-consistency filter and point fusion over the stream,
+                                as the reference's cleaner and pruner queues do
+                                (depthmap_computation_module.cc:396-412, dense_pointcloud_module.cc:115-175):
+                                keyframe k's depth is cleaned against the two densified keyframes of its size
+                                before and after it, and its cleaned map is fused against the next four
+                                cleaned maps; results through pm_server_wait_dense */
+    float clean_threshold;   /* filter: relative depth agreement (0.01, DepthmapCleaner default) */
+    int clean_min_views;     /* filter: consistent views including itself (3) */
+    float clean_reproj_px;   /* filter: round-trip reprojection test in pixels (1.0; 0 = off) */
+    float fuse_threshold;    /* fusion: relative depth threshold (0.08, Dense.SameDepthThreshold of the
+                                reference's example configuration) */
+    float min_view_score;    /* keyframes submitted with landmarks join only when score_view against the
+                                previous joined keyframe exceeds this (0.25, :334-335) */
 } pm_server_config;
 typedef struct {
     int status;              /* PM_OK, PM_ENOTREADY (too few neighbours) or an error */
@@ -362,6 +383,7 @@ typedef struct {
     int iterations;
     double queue_ms;         /* submit -> start on the GPU */
     double latency_ms;       /* submit -> maps on the host */
+    float view_score;        /* score_view against the previous joined keyframe (-1: not computed) */
 } pm_served_info;
 /* Memory: requests and retained results (20 B/px, at most prior_lag + 1 per
  * image size) are admitted against the context's HBM budget; the keyframe
@@ -371,6 +393,17 @@ void pm_server_config_default(pm_server_config *cfg);
 int pm_server_create(pm_ctx *ctx, const pm_server_config *cfg, pm_server **out);
 /* Copies the keyframe's gray image (uint8) and pose; returns a ticket. */
 int pm_server_submit(pm_server *srv, int width, int height, const pm_view *keyframe, uint64_t *ticket);
+/* The same with the keyframe's SLAM landmarks (world points xyz[n x 3], FP64,
+ * and their ids), as the reference's densification thread receives them
+ * (depthmap_computation_module.cc:328-374): the keyframe joins only when
+ * score_view against the previous joined keyframe with landmarks exceeds
+ * min_view_score (otherwise it completes with PM_ENOTREADY and is neither
+ * cached nor densified), its depth interval's upper bound becomes 1.1 x the
+ * 90th percentile of the landmark ranges (compute_depth_intervall, :123-131;
+ * the lower bound stays params.min_depth), and it is seeded from the
+ * landmarks before any prior result (PreInitSparsePCL2, depthmap.cc:361-432). */
+int pm_server_submit_landmarks(pm_server *srv, int width, int height, const pm_view *keyframe,
+                               const double *xyz_world, const uint64_t *ids, int n_landmarks, uint64_t *ticket);
 /* Blocks until the ticket's keyframe is done (timeout_ms < 0: no limit;
  * PM_ETIMEOUT otherwise), then fills out->depth / out->score (host, may be
  * NULL) and info.  Returns the keyframe's status.  Each ticket is collected
@@ -378,7 +411,27 @@ int pm_server_submit(pm_server *srv, int width, int height, const pm_view *keyfr
  * collected (also when another thread collects it while this one waits).
  * All waits must have returned before pm_server_destroy. */
 int pm_server_wait(pm_server *srv, uint64_t ticket, int timeout_ms, pm_maps *out, pm_served_info *info);
-/* Finishes all submitted keyframes, then releases everything. */
+/* With dense_output: blocks until the ticket's fused output exists (timeout as
+ * pm_server_wait), then fills depth (H x W host floats: the keyframe's depth
+ * after the consistency filter and fusion, may be NULL) and points (host:
+ * xyz world FP64 and ij (row, col) of the points fusion kept, up to
+ * points->capacity; points->count receives the total, PM_EINVAL when it
+ * exceeds the capacity; bgr is not written, the served loop receives gray
+ * images).  Returns PM_OK, PM_ENOTREADY for a keyframe that was not densified
+ * or whose filter or fusion window never filled (the first two and the last
+ * keyframes of each image size, as in the reference), PM_ECANCELLED for one
+ * cancelled by pm_server_destroy, or PM_EINVAL (no dense output, unknown or
+ * already collected ticket).  Collected once, independently of pm_server_wait. */
+int pm_server_wait_dense(pm_server *srv, uint64_t ticket, int timeout_ms, float *depth, pm_points *points);
+/* End of the stream: refuses further submissions (PM_ECANCELLED), densifies
+ * every keyframe already submitted, completes every dense output (those whose
+ * windows never filled with PM_ENOTREADY) and returns when all results exist;
+ * they stay collectable until pm_server_destroy. */
+int pm_server_finish(pm_server *srv);
+/* Finishes the keyframes already on the GPU; keyframes still queued complete
+ * with PM_ECANCELLED (and their dense outputs too).  Returns once every thread
+ * blocked in pm_server_wait / pm_server_wait_dense has returned; no call may
+ * use the server afterwards.  Uncollected results are released. */
 int pm_server_destroy(pm_server *srv);
 
 /* ---- fusion for callers that cannot allocate device memory ----

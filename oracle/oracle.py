@@ -17,7 +17,7 @@ LIB = os.path.join(BUILD_DIR, "liboracle.so")
 
 OR_MAX_VIEWS = 17
 COMBINE_FOLD, COMBINE_MAX, COMBINE_TOPK, COMBINE_FOLD_SEPARATE = 0, 1, 2, 3
-SEAM_CLAMP, SEAM_WRAP = 0, 1
+SEAM_CLAMP, SEAM_WRAP, SEAM_ZERO = 0, 1, 2
 ARITH_F64, ARITH_F32_REF = 0, 1
 INTERP_EXACT, INTERP_TEX8_RN, INTERP_TEX8_RZ = 0, 1, 2
 PROP_SMOOTH, PROP_PLAIN = 0, 1

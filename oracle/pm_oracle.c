@@ -131,6 +131,7 @@ static double bilinear64(const float *img, int W, int H, double u, double v, int
 {
     if (!isfinite(u)) u = 0.0;
     if (!isfinite(v)) v = 0.0;
+    if (seam == OR_SEAM_ZERO && (u < 0.0 || u >= W - 1 || v < 0.0 || v >= H - 1)) return 0.0;
     u = u < 0.0 ? 0.0 : (u > W ? (double)W : u);
     v = v < 0.0 ? 0.0 : (v > H ? (double)H : v);
     u = quantize_coord(u, interp);
@@ -149,6 +150,7 @@ static float bilinear32(const float *img, int W, int H, float u, float v, int se
 {
     if (!isfinite(u)) u = 0.0f;
     if (!isfinite(v)) v = 0.0f;
+    if (seam == OR_SEAM_ZERO && (u < 0.0f || u >= W - 1 || v < 0.0f || v >= H - 1)) return 0.0f;
     u = u < 0.0f ? 0.0f : (u > (float)W ? (float)W : u);
     v = v < 0.0f ? 0.0f : (v > (float)H ? (float)H : v);
     if (interp != OR_INTERP_EXACT) {
@@ -259,6 +261,7 @@ static double cost_f64(const or_views *v, const or_cost_params *p, int i, int j,
                 for (int a = 0; a < 3; ++a)
                     X[a] = M[3 * a] * Xc[0] + M[3 * a + 1] * Xc[1] + M[3 * a + 2] * Xc[2] + c[a];
                 double d = sqrt(X[0] * X[0] + X[1] * X[1] + X[2] * X[2]);
+                if (p->seam == OR_SEAM_ZERO && d < 1e-4) continue;  /* too near: skipped (depthmap.cc:147-149) */
                 double sc = 1.0 / fmax(1e-6, d);
                 double bx = X[0] * sc, by = X[1] * sc, bz = X[2] * sc;
                 if (by > 1.0) by = 1.0;
@@ -275,7 +278,7 @@ static double cost_f64(const or_views *v, const or_cost_params *p, int i, int j,
         }
         double mx = swx / sw, my = swy / sw;
         double vx = swxx / sw - mx * mx, vy = swyy / sw - my * my;
-        ncc[r] = (vx < 0.1 || vy < 0.1) ? -1.0 : (swxy / sw - mx * my) / sqrt(vx * vy);
+        ncc[r] = (sw == 0.0 || vx < 0.1 || vy < 0.1) ? -1.0 : (swxy / sw - mx * my) / sqrt(vx * vy);
         c_sw += sw; c_swx += swx; c_swy += swy; c_swxx += swxx; c_swyy += swyy; c_swxy += swxy;
         mx = c_swx / c_sw; my = c_swy / c_sw;
         vx = c_swxx / c_sw - mx * mx; vy = c_swyy / c_sw - my * my;

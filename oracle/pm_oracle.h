@@ -57,7 +57,11 @@ typedef struct {
  * NCC covers the samples of views 1..r, folded with the 25 % rule.
  * OR_COMBINE_FOLD_SEPARATE folds independent per-view NCCs instead. */
 enum { OR_COMBINE_FOLD = 0, OR_COMBINE_MAX = 1, OR_COMBINE_TOPK = 2, OR_COMBINE_FOLD_SEPARATE = 3 };
-enum { OR_SEAM_CLAMP = 0, OR_SEAM_WRAP = 1 };
+/* OR_SEAM_ZERO is the reference host cost (ComputePlaneImageScoreUnoptimized_equirect,
+ * depthmap.cc:1129-1157): LinearInterpolation returns 0 for a sample outside
+ * [0, W-1) x [0, H-1) (depthmap.cc:34-38), and a sample whose point lies within
+ * 1e-4 of the source camera is skipped (ReprojectEquirect, depthmap.cc:143-150). */
+enum { OR_SEAM_CLAMP = 0, OR_SEAM_WRAP = 1, OR_SEAM_ZERO = 2 };
 /* OR_ARITH_F64: exact (double) arithmetic and exact bilinear interpolation.
  * OR_ARITH_F32_REF: the reference kernel's own float arithmetic, step by step
  * (PatchMatchCuda.cu:97-178): normalised float bearing table, two-step pose

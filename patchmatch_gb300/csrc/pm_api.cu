@@ -172,7 +172,8 @@ int validate_params(pm_ctx *ctx, const pm_params *p) {
     if (p->iterations < 0 || p->iterations > 1000) return fail(ctx, PM_EINVAL, "iterations out of range");
     if (p->combine < PM_COMBINE_FOLD || p->combine > PM_COMBINE_FOLD_SEPARATE) return fail(ctx, PM_EINVAL, "bad combine");
     if (p->top_k < 1) return fail(ctx, PM_EINVAL, "top_k must be >= 1");
-    if (p->seam != PM_SEAM_CLAMP && p->seam != PM_SEAM_WRAP) return fail(ctx, PM_EINVAL, "bad seam");
+    if (p->seam != PM_SEAM_CLAMP && p->seam != PM_SEAM_WRAP && p->seam != PM_SEAM_ZERO)
+        return fail(ctx, PM_EINVAL, "bad seam");
     if (p->init_mode != PM_INIT_LOGUNIFORM_HEMI && p->init_mode != PM_INIT_REF_UNIFORM)
         return fail(ctx, PM_EINVAL, "bad init_mode");
     if (p->image_format != PM_IMAGE_U8 && p->image_format != PM_IMAGE_F16)
@@ -1292,6 +1293,8 @@ int pm_request_synchronize(pm_request *r) {
 }
 
 const float *pm_request_depth_device(const pm_request *r) { return r ? r->fdepth : nullptr; }
+
+const float *pm_result_depth_device(const pm_result *res) { return res ? res->fdepth : nullptr; }
 
 void *pm_request_stream(const pm_request *r) { return r ? (void *)r->stream : nullptr; }
 

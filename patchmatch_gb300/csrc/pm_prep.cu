@@ -31,6 +31,13 @@ __global__ void build_quad_kernel(const uint8_t *raw, size_t pitch, int fmt, int
     }
     const int ya = min(y, H - 1), yb = min(y + 1, H - 1);
     const size_t qi = (size_t)y * (W + 1) + x;
+    if (seam == PM_SEAM_ZERO && (x >= W - 1 || y >= H - 1)) {
+        // a sample whose footprint leaves [0, W-1) x [0, H-1) reads 0
+        // (LinearInterpolation, depthmap.cc:34-38): the whole cell is 0
+        if (fmt == PM_IMAGE_U8) static_cast<uint32_t *>(quad)[qi] = 0u;
+        else static_cast<uint2 *>(quad)[qi] = make_uint2(0u, 0u);
+        return;
+    }
     if (fmt == PM_IMAGE_U8) {
         const uint8_t *r0 = raw + (size_t)ya * pitch, *r1 = raw + (size_t)yb * pitch;
         const uint32_t w = (uint32_t)r0[xa] | ((uint32_t)r0[xb] << 8) | ((uint32_t)r1[xa] << 16) |

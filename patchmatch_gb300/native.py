@@ -14,7 +14,7 @@ from ._native import load_pm_lib
 
 PM_OK, PM_EINVAL, PM_ENOMEM, PM_EBUDGET, PM_ETIMEOUT, PM_ECUDA, PM_ENOTREADY, PM_ECANCELLED, PM_ENOTBUILT = range(9)
 COMBINE_FOLD, COMBINE_MAX, COMBINE_TOPK, COMBINE_FOLD_SEPARATE = 0, 1, 2, 3
-SEAM_CLAMP, SEAM_WRAP = 0, 1
+SEAM_CLAMP, SEAM_WRAP, SEAM_ZERO = 0, 1, 2
 INIT_LOGUNIFORM_HEMI, INIT_REF_UNIFORM = 0, 1
 IMAGE_U8, IMAGE_F16 = 0, 1
 SAMPLER_EXACT, SAMPLER_TEXTURE = 0, 1
@@ -41,6 +41,7 @@ EXPORTS = (
     "pm_filter_consistency_device", "pm_fuse_workspace_bytes", "pm_fuse_device", "pm_probe_sfu_peak",
     "pm_probe_tex_peak",
     "pm_server_config_default", "pm_server_create", "pm_server_submit", "pm_server_wait", "pm_server_destroy",
+    "pm_server_submit_landmarks", "pm_server_wait_dense", "pm_result_depth_device", "pm_server_finish",
 )
 
 
@@ -71,7 +72,9 @@ class ServerConfig(C.Structure):
     _fields_ = [("params", Params), ("cache_capacity", C.c_int), ("max_inflight", C.c_int),
                 ("min_sources", C.c_int), ("max_sources", C.c_int), ("min_baseline", C.c_float),
                 ("max_baseline", C.c_float), ("seed_from_prior", C.c_int), ("seeded_iterations", C.c_int),
-                ("prior_lag", C.c_int), ("poll_us", C.c_int), ("coarse_to_fine", C.c_int)]
+                ("prior_lag", C.c_int), ("poll_us", C.c_int), ("coarse_to_fine", C.c_int),
+                ("dense_output", C.c_int), ("clean_threshold", C.c_float), ("clean_min_views", C.c_int),
+                ("clean_reproj_px", C.c_float), ("fuse_threshold", C.c_float), ("min_view_score", C.c_float)]
 
 
 class BatchTuning(C.Structure):
@@ -80,7 +83,7 @@ class BatchTuning(C.Structure):
 
 class ServedInfo(C.Structure):
     _fields_ = [("status", C.c_int), ("n_sources", C.c_int), ("seeded", C.c_int), ("iterations", C.c_int),
-                ("queue_ms", C.c_double), ("latency_ms", C.c_double)]
+                ("queue_ms", C.c_double), ("latency_ms", C.c_double), ("view_score", C.c_float)]
 
 
 _vp, _sz = C.c_void_p, C.c_size_t
@@ -167,6 +170,12 @@ def lib():
     L.pm_server_create.argtypes = [_vp, C.POINTER(ServerConfig), C.POINTER(_vp)]
     L.pm_server_submit.argtypes = [_vp, C.c_int, C.c_int, C.POINTER(View), C.POINTER(C.c_uint64)]
     L.pm_server_wait.argtypes = [_vp, C.c_uint64, C.c_int, C.POINTER(Maps), C.POINTER(ServedInfo)]
+    L.pm_server_submit_landmarks.argtypes = [_vp, C.c_int, C.c_int, C.POINTER(View), _vp, _vp, C.c_int,
+                                             C.POINTER(C.c_uint64)]
+    L.pm_server_wait_dense.argtypes = [_vp, C.c_uint64, C.c_int, _vp, C.POINTER(Points)]
+    L.pm_server_finish.argtypes = [_vp]
+    L.pm_result_depth_device.restype = _vp
+    L.pm_result_depth_device.argtypes = [_vp]
     L.pm_server_destroy.argtypes = [_vp]
     L._pm_typed = True
     return L
@@ -676,6 +685,7 @@ class Server:
             raise PmError(rc, "pm_server_create failed")
         self.h = h.value
         self.shape = {}
+        self.dense_shape = {}
 
     def submit(self, gray, R, t) -> int:
         gray = np.ascontiguousarray(gray, np.uint8)
@@ -686,7 +696,42 @@ class Server:
         if rc != PM_OK:
             raise PmError(rc, "pm_server_submit failed")
         self.shape[tk.value] = (H, W)
+        self.dense_shape[tk.value] = (H, W)
         return tk.value
+
+    def submit_landmarks(self, gray, R, t, xyz, ids) -> int:
+        """pm_server_submit_landmarks: the keyframe with its SLAM landmarks (world xyz, ids)."""
+        gray = np.ascontiguousarray(gray, np.uint8)
+        H, W = gray.shape
+        v = make_view(gray, R, t)
+        xyz = np.ascontiguousarray(xyz, np.float64).reshape(-1, 3)
+        ids = np.ascontiguousarray(ids, np.uint64)
+        if len(ids) != len(xyz):
+            raise ValueError("xyz and ids differ in length")
+        tk = C.c_uint64()
+        rc = self._L.pm_server_submit_landmarks(self.h, W, H, C.byref(v), _ptr(xyz), _ptr(ids), len(ids),
+                                                C.byref(tk))
+        if rc != PM_OK:
+            raise PmError(rc, "pm_server_submit_landmarks failed")
+        self.shape[tk.value] = (H, W)
+        self.dense_shape[tk.value] = (H, W)
+        return tk.value
+
+    def wait_dense(self, ticket: int, timeout_ms: int = -1):
+        """pm_server_wait_dense: (status, fused depth or None, xyz[n,3] f64 or None, ij[n,2] or None)."""
+        H, W = self.dense_shape[ticket]
+        depth = np.zeros((H, W), np.float32)
+        cap = H * W
+        xyz = np.zeros((cap, 3), np.float64)
+        ij = np.zeros((cap, 2), np.int32)
+        pts = Points(cap, 0, xyz.ctypes.data, None, ij.ctypes.data)
+        rc = self._L.pm_server_wait_dense(self.h, ticket, timeout_ms, depth.ctypes.data, C.byref(pts))
+        if rc != PM_ETIMEOUT:
+            self.dense_shape.pop(ticket, None)
+        if rc != PM_OK:
+            return rc, None, None, None
+        n = pts.count
+        return rc, depth, xyz[:n], ij[:n]
 
     def wait(self, ticket: int, timeout_ms: int = -1, want_score: bool = False):
         """Returns (status, depth or None, score or None, info dict)."""
@@ -703,6 +748,12 @@ class Server:
         d = {k: getattr(info, k) for k, _ in ServedInfo._fields_}
         ok = rc == PM_OK
         return rc, (depth if ok else None), (score if ok else None), d
+
+    def finish(self):
+        """pm_server_finish: end of stream, every result completes and stays collectable."""
+        rc = self._L.pm_server_finish(self.h)
+        if rc != PM_OK:
+            raise PmError(rc, "pm_server_finish failed")
 
     def close(self):
         if getattr(self, "h", None):

@@ -90,6 +90,41 @@ def test_fixed_hypotheses_wrap_seam_and_f16(ctx):
             r.close()
 
 
+def test_host_cost_mode_matches_oracle(ctx):
+    """The reference's host cost (ComputePlaneImageScoreUnoptimized_equirect
+    with ComputePlaneScore's maximum over views, depthmap.cc:1104-1157):
+    PM_SAMPLER_EXACT + PM_SEAM_ZERO + PM_COMBINE_MAX, whose samples read 0
+    once their footprint leaves [0, W-1) x [0, H-1).  Hypotheses at pixels next
+    to the seam and the poles, where that border decides the cost, against the
+    oracle's restatement; the best view is the argmax (the reference's nghbr)."""
+    req = scene.make_request(scene.ROOM, W1, H1, 4, seed=17)
+    rng = np.random.default_rng(9)
+    n = 6000
+    cols = np.concatenate([rng.integers(6, 24, n // 2), rng.integers(W1 - 24, W1 - 6, n // 2)])
+    rows = np.where(rng.random(n) < 0.5, rng.integers(6, 24, n), rng.integers(H1 - 24, H1 - 6, n))
+    rows = np.where(rng.random(n) < 0.3, rng.integers(6, H1 - 6, n), rows)
+    ij = np.stack([rows, cols], 1).astype(np.int32)
+    v0 = req.views[0]
+    gt = np.array([O.gt_plane(v0.depth[i, j], v0.normal[i, j], W1, H1, i, j) for i, j in ij], np.float32)
+    planes = (gt * rng.uniform(0.8, 1.25, (n, 1))).astype(np.float32)
+    r = _req_on_gpu(ctx, req, combine=native.COMBINE_MAX, seam=native.SEAM_ZERO)
+    g, gb, gps = r.score_hypotheses(ij, planes, per_source=True)
+    r.close()
+    V = O.Views.from_request(req)
+    o, ob, ops = O.cost_batch(V, O.cost_params(combine=O.COMBINE_MAX, seam=O.SEAM_ZERO), ij, planes, want_ncc=True)
+    _, _, oclamp = O.cost_batch(V, O.cost_params(combine=O.COMBINE_MAX, seam=O.SEAM_CLAMP), ij, planes,
+                                want_ncc=True)
+    err = np.abs(gps - ops)
+    frac = (err <= 1e-5 * np.maximum(1.0, np.abs(ops))).mean()
+    differs = (np.abs(ops - oclamp) > 1e-3).mean()
+    print(f"host cost mode: per-source within 1e-5 {frac:.5f}, median {np.median(err):.2e}; "
+          f"border changes {differs:.3f} of the per-source costs against a clamped border")
+    assert differs > 0.02  # the border matters for these pixels
+    assert frac >= 0.995
+    assert np.abs(g - o).max() <= 1e-3
+    assert ((gb == ob) | (np.abs(np.take_along_axis(ops, gb[:, None], 1)[:, 0] - ops.max(1)) < 1e-4)).mean() >= 0.999
+
+
 @pytest.mark.parametrize("n_src", [1, 2, 7, 10])
 def test_source_counts(ctx, n_src):
     req = scene.make_request(scene.ROOM, 128, 64, n_src, seed=20 + n_src)

@@ -139,3 +139,19 @@ def test_landmark_candidates_restatement():
     assert c[10, 20, 3] == np.float32(2.0)
     assert np.allclose(c[10, 20, :3], b / 2.0, rtol=1e-6)
     assert (c[..., 3] > 0).sum() == 1
+
+
+def test_host_cost_border_reads_zero(room):
+    """OR_SEAM_ZERO restates the reference host cost's border
+    (LinearInterpolation, depthmap.cc:34-38): a sample whose footprint leaves
+    [0, W-1) x [0, H-1) reads 0.  Hypotheses whose samples all stay inside
+    score the same as with a clamped border; at the seam columns they differ."""
+    H, W = room.H, room.W
+    V = O.Views.from_request(room)
+    v0 = room.views[0]
+    ij = np.array([[H // 2, W // 2], [H // 2, 6], [H // 2, W - 7], [H // 3, W - 7]], np.int32)
+    planes = np.array([O.gt_plane(v0.depth[i, j], v0.normal[i, j], W, H, i, j) for i, j in ij], np.float32)
+    _, _, z = O.cost_batch(V, O.cost_params(seam=O.SEAM_ZERO, combine=O.COMBINE_MAX), ij, planes, want_ncc=True)
+    _, _, c = O.cost_batch(V, O.cost_params(seam=O.SEAM_CLAMP, combine=O.COMBINE_MAX), ij, planes, want_ncc=True)
+    assert np.allclose(z[0], c[0], rtol=0, atol=1e-12)  # image centre: every sample inside
+    assert np.abs(z[1:] - c[1:]).max() > 1e-3           # at the seam the border decides
