@@ -1217,10 +1217,12 @@ int pm_request_postprocess(pm_request *r) {
 int pm_request_run(pm_request *r) {
     if (!r) return PM_EINVAL;
     pm_ctx *ctx = r->ctx;
+    NvtxRange range("pm_request_run %dx%d S=%d sweeps=%d", r->W, r->H, r->S, r->prm.iterations);
     int rc = check_views(r);
     if (rc) return rc;
     PM_CUDA(ctx, cudaSetDevice(ctx->device));
     if (r->graph_dirty || !r->gexec) {
+        NvtxRange capture("capture sweep graph");
         fill_args(r);
         cudaGraph_t g = nullptr;
         PM_CUDA(ctx, cudaStreamBeginCapture(r->stream, cudaStreamCaptureModeThreadLocal));
@@ -1417,6 +1419,7 @@ static int filter_check(pm_ctx *ctx, int W, int H, int n, const float *const *de
 static int enqueue_filter(pm_ctx *ctx, int W, int H, int n, const float *const *depths, const double *R,
                           const double *t, int center, float thr, int min_consistent, float reproj_px, float *out,
                           cudaStream_t st) {
+    NvtxRange range("consistency filter %dx%d views=%d", W, H, n);
     Trig tr;
     int rc = get_trig(ctx, W, H, &tr);
     if (rc) return rc;
@@ -1485,6 +1488,7 @@ static int fuse_check(pm_ctx *ctx, int W, int H, int n, float *const *depths, co
 static int enqueue_fuse(pm_ctx *ctx, int W, int H, int n, float *const *depths, const double *R, const double *t,
                         const uint8_t *bgr, float thr, float *pruned, float *xyz, uint8_t *bgr_out, int32_t *ij,
                         unsigned *count, void *ws, cudaStream_t st) {
+    NvtxRange range("fusion %dx%d views=%d", W, H, n);
     Trig tr;
     int rc = get_trig(ctx, W, H, &tr);
     if (rc) return rc;

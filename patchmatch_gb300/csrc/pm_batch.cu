@@ -293,6 +293,7 @@ int pm_batch_set_executor(pm_batch *b, int executor, int grid_mult) {
 int pm_batch_run(pm_batch *b) {
     if (!b) return PM_EINVAL;
     pm_ctx *ctx = b->ctx;
+    NvtxRange range("pm_batch_run requests=%d", (int)b->reqs.size());
     if (b->reqs.empty()) return fail(ctx, PM_EINVAL, "empty batch");
     for (pm_request *r : b->reqs) {
         int rc = check_views(r);

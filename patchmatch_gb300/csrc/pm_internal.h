@@ -15,6 +15,24 @@
 
 #define PM_INTERNAL __attribute__((visibility("hidden")))
 
+#include <nvtx3/nvToolsExt.h>
+
+// An NVTX range over a host-side scope (visible in Nsight timelines; a no-op
+// unless a tool is attached).
+struct NvtxRange {
+    explicit NvtxRange(const char *fmt, ...) {
+        char buf[128];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        nvtxRangePushA(buf);
+    }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
+
 // Bearing tables of one image size (device).
 struct Trig {
     int W = 0, H = 0;

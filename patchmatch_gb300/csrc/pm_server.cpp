@@ -27,6 +27,8 @@
 
 #include <cuda_runtime.h>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "pm_gb300.h"
 
 namespace {
@@ -453,6 +455,10 @@ void prune_priors(pm_server *s, uint64_t next) {
 
 // Start one submission on the GPU; returns PM_EBUDGET when it must wait.
 int start_job(pm_server *s, Submission &sub, CachedKeyframe *kf) {
+    nvtxRangePushA("served keyframe start");
+    struct Pop {
+        ~Pop() { nvtxRangePop(); }
+    } pop;
     std::vector<const CachedKeyframe *> src = select_sources(s, *kf);
     if ((int)src.size() < s->cfg.min_sources) {
         Result r;
