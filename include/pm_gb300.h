@@ -479,8 +479,14 @@ int pm_fuse_noalloc(int width, int height, int n_views, float *const *depths, co
  * of all counts, at the register budget of the largest).  Every request's maps equal those of
  * pm_request_run bit for bit.  Requests keep their own buffers and streams:
  * set their views before pm_batch_run; read them afterwards with
- * pm_request_read (their streams wait for the batch).  Seeding (priors,
- * landmarks) is not batched (PM_EINVAL).  A request in a batch cannot be
+ * pm_request_read (their streams wait for the batch).  Seeded requests are
+ * batched too: landmark seeds and priors (a retained result, a request outside
+ * the batch, or a request of the same batch, e.g. a coarse-to-fine chain whose
+ * full-size request is seeded from a half-size one) are applied between the
+ * init scoring and the sweeps as pm_request_run does; a request seeded from a
+ * member runs one level after it (levels run in order, each level
+ * phase-major), and priors from outside the batch are waited for before the
+ * graph starts.  A cycle of priors within a batch is PM_EINVAL.  A request in a batch cannot be
  * destroyed (pm_request_destroy returns PM_EINVAL) until pm_batch_clear or
  * pm_batch_destroy releases it.  pm_batch_tune runs the batch once
  * per executor candidate, keeps the fastest and reports the timings.

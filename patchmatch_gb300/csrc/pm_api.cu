@@ -350,7 +350,8 @@ void set_tile_order(pm_request *r) {
     r->banded_blocks = bps > 0 ? bps * r->ctx->n_sm : 0;
 }
 
-int launch_tile(pm_request *r, int mode, int colour, int sweep) {
+int launch_tile(pm_request *r, int mode, int colour, int sweep, cudaStream_t st = nullptr) {
+    if (!st) st = r->stream;
     pm::SweepArgs a = r->args;
     a.mode = mode;
     a.colour = colour;
@@ -359,9 +360,9 @@ int launch_tile(pm_request *r, int mode, int colour, int sweep) {
     const dim3 grid = pm::tile_grid(r->W, r->H);
     pm::BandArgs band{};
     const pm::BandArgs *bp = nullptr;
-    const int rc = pmi::tile_band(r, grid, r->stream, &band, &bp);
+    const int rc = pmi::tile_band(r, grid, st, &band, &bp);
     if (rc) return rc;
-    cudaError_t e = pm::dispatch_tile(r->S, kind, grid, r->stream, a, bp);
+    cudaError_t e = pm::dispatch_tile(r->S, kind, grid, st, a, bp);
     r->ctx->launches++;
     if (e != cudaSuccess) return fail(r->ctx, PM_ECUDA, "tile kernel launch: %s", cudaGetErrorString(e));
     return PM_OK;
@@ -435,7 +436,7 @@ struct PriorSrc {
     const double *R, *t;
 };
 
-int enqueue_seed_from(pm_request *r, const PriorSrc &prior) {
+int enqueue_seed_from(pm_request *r, const PriorSrc &prior, cudaStream_t st) {
     pm::WarpArgs w{};
     w.prev_plane = prior.plane;
     w.prev_depth = prior.fdepth;
@@ -452,32 +453,37 @@ int enqueue_seed_from(pm_request *r, const PriorSrc &prior) {
     w.col = r->trig.col;
     w.zbuf = r->zbuf;
     w.seed = r->seed;
-    pm::launch_warp_prior(r->stream, w);
+    pm::launch_warp_prior(st, w);
     r->ctx->launches += 2;
     for (int c = 0; c < 2; ++c) {
-        int rc = launch_tile(r, pm::kModeSeed, c, 0);
+        int rc = launch_tile(r, pm::kModeSeed, c, 0, st);
         if (rc) return rc;
     }
     return PM_OK;
 }
 
-int enqueue_seed(pm_request *r, const pm_request *prior) {
-    if (!prior->postprocessed) return fail(r->ctx, PM_EINVAL, "prior request has no post-filtered result");
+// `postprocessed` is false for a prior that runs later in the same batch
+// (its post-filter is enqueued before this seeding there).
+int enqueue_seed(pm_request *r, const pm_request *prior, cudaStream_t st = nullptr, bool in_batch = false) {
+    if (!prior->postprocessed && !(in_batch && prior->prm.postprocess))
+        return fail(r->ctx, PM_EINVAL, "prior request has no post-filtered result");
     return enqueue_seed_from(r, PriorSrc{prior->plane, prior->fdepth, prior->W, prior->H, prior->trig, prior->R[0],
-                                         prior->t[0]});
+                                         prior->t[0]}, st ? st : r->stream);
 }
 
-int enqueue_seed_result(pm_request *r, const pm_result *res) {
+int enqueue_seed_result(pm_request *r, const pm_result *res, cudaStream_t st = nullptr) {
     if (!res->valid) return fail(r->ctx, PM_EINVAL, "prior result holds no snapshot");
-    return enqueue_seed_from(r, PriorSrc{res->plane, res->fdepth, res->W, res->H, res->trig, res->R, res->t});
+    return enqueue_seed_from(r, PriorSrc{res->plane, res->fdepth, res->W, res->H, res->trig, res->R, res->t},
+                             st ? st : r->stream);
 }
 
-int enqueue_landmarks(pm_request *r) {
-    pm::launch_landmark_cands(r->stream, r->lm, r->n_lm, r->has_mask ? r->mask : nullptr, r->trig.row, r->trig.col,
+int enqueue_landmarks(pm_request *r, cudaStream_t st = nullptr) {
+    if (!st) st = r->stream;
+    pm::launch_landmark_cands(st, r->lm, r->n_lm, r->has_mask ? r->mask : nullptr, r->trig.row, r->trig.col,
                               r->W, r->H, r->seed);
     r->ctx->launches += r->n_lm > 0 ? 1 : 0;
     for (int c = 0; c < 2; ++c) {
-        int rc = launch_tile(r, pm::kModeSeed, c, 0);
+        int rc = launch_tile(r, pm::kModeSeed, c, 0, st);
         if (rc) return rc;
     }
     return PM_OK;
@@ -537,6 +543,27 @@ int stage_landmarks(pm_request *r, const double *xyz, int n) {
     r->n_lm = (int)list.size();
     return PM_OK;
 }
+
+}  // namespace
+
+int pmi::enqueue_seeding(pm_request *r, cudaStream_t st, bool in_batch) {
+    int rc = PM_OK;
+    if (r->n_lm > 0) rc = enqueue_landmarks(r, st);
+    if (!rc && r->prior) rc = enqueue_seed(r, r->prior, st, in_batch);
+    else if (!rc && r->prior_res) rc = enqueue_seed_result(r, r->prior_res, st);
+    return rc;
+}
+
+int pmi::wait_prior_ready(pm_request *r, cudaStream_t st) {
+    if (r->prior && r->prior->stream != st) {
+        PM_CUDA(r->ctx, cudaEventRecord(r->prior->ready, r->prior->stream));
+        PM_CUDA(r->ctx, cudaStreamWaitEvent(st, r->prior->ready, 0));
+    }
+    if (r->prior_res) PM_CUDA(r->ctx, cudaStreamWaitEvent(st, r->prior_res->ready, 0));
+    return PM_OK;
+}
+
+namespace {
 
 int enqueue_run(pm_request *r) {
     int rc = enqueue_init(r);

@@ -29,6 +29,7 @@ using pmi::fill_args;
 struct pm_batch {
     struct Group {
         int S = 0, kind = 0, iterations = 0;
+        int level = 0;  // seeding level: requests seeded from a batch member run one level after it
         bool plain = false;
         std::vector<pm_request *> members;
         pm::SweepArgs *d_args = nullptr;
@@ -54,6 +55,8 @@ struct pm_batch {
     int executor = PM_BATCH_PERSISTENT;
     int grid_mult = 1;
     uint64_t launches_per_run = 0;
+    std::vector<int> level;        // per request (index into reqs)
+    int n_levels = 1;
 };
 
 namespace {
@@ -67,17 +70,50 @@ void batch_free_groups(pm_batch *b) {
     b->groups.clear();
 }
 
+int batch_index(const pm_batch *b, const pm_request *r) {
+    for (size_t k = 0; k < b->reqs.size(); ++k)
+        if (b->reqs[k] == r) return (int)k;
+    return -1;
+}
+
+// Seeding levels: 0 for a request without a prior in the batch, else one more
+// than its prior's.  A cycle of priors inside the batch is rejected.
+int batch_levels(pm_batch *b) {
+    const size_t n = b->reqs.size();
+    b->level.assign(n, 0);
+    b->n_levels = 1;
+    for (size_t k = 0; k < n; ++k) {
+        int lv = 0;
+        const pm_request *r = b->reqs[k];
+        for (size_t hop = 0; hop <= n; ++hop) {
+            const int p = r->prior ? batch_index(b, r->prior) : -1;
+            if (p < 0) break;
+            if (hop == n) return fail(b->ctx, PM_EINVAL, "the priors of the batch's requests form a cycle");
+            ++lv;
+            r = b->reqs[p];
+        }
+        b->level[k] = lv;
+        b->n_levels = std::max(b->n_levels, lv + 1);
+    }
+    return PM_OK;
+}
+
 int batch_build(pm_batch *b) {
     pm_ctx *ctx = b->ctx;
     batch_free_groups(b);
-    for (pm_request *r : b->reqs) {
+    int rc0 = batch_levels(b);
+    if (rc0) return rc0;
+    for (size_t k = 0; k < b->reqs.size(); ++k) {
+        pm_request *r = b->reqs[k];
         const int kind = pm::image_kind(r->prm.image_format, r->prm.sampler);
         const bool plain = r->prm.propagation == PM_PROPAGATION_PLAIN;
         pm_batch::Group *g = nullptr;
         // the mixed kernel takes every source count in one group (S = 0)
         const int gS = b->executor == PM_BATCH_MIXED ? 0 : r->S;
         for (auto &x : b->groups)
-            if (x.S == gS && x.kind == kind && x.plain == plain && x.iterations == r->prm.iterations) g = &x;
+            if (x.S == gS && x.kind == kind && x.plain == plain && x.iterations == r->prm.iterations &&
+                x.level == b->level[k])
+                g = &x;
         if (!g) {
             b->groups.emplace_back();
             g = &b->groups.back();
@@ -85,6 +121,7 @@ int batch_build(pm_batch *b) {
             g->kind = kind;
             g->plain = plain;
             g->iterations = r->prm.iterations;
+            g->level = b->level[k];
         }
         g->members.push_back(r);
     }
@@ -109,6 +146,14 @@ int batch_build(pm_batch *b) {
     return PM_OK;
 }
 
+// Seeding of r on st inside the batch's graph; its launches are counted in `launches`.
+int seed_in_batch(pm_batch *b, pm_request *r, cudaStream_t st, uint64_t &launches) {
+    const uint64_t before = b->ctx->launches;
+    const int rc = pmi::enqueue_seeding(r, st, r->prior && batch_index(b, r->prior) >= 0);
+    launches += b->ctx->launches - before;
+    return rc;
+}
+
 int batch_enqueue(pm_batch *b) {
     pm_ctx *ctx = b->ctx;
     const cudaStream_t st = b->stream;
@@ -124,20 +169,34 @@ int batch_enqueue(pm_batch *b) {
         // each request's whole chain on one of the branch streams (largest
         // first onto the least-loaded branch), branches forked from and
         // joined back into the batch stream
-        std::vector<pm_request *> order = b->reqs;
-        std::sort(order.begin(), order.end(), [](const pm_request *x, const pm_request *y) {
-            return (double)x->W * x->H * x->S * (1 + x->prm.iterations) >
-                   (double)y->W * y->H * y->S * (1 + y->prm.iterations);
+        // seeded requests follow their prior (lower level first) on the prior's branch
+        std::vector<int> order(b->reqs.size());
+        for (size_t k = 0; k < order.size(); ++k) order[k] = (int)k;
+        auto work = [&](int k) {
+            const pm_request *x = b->reqs[k];
+            return (double)x->W * x->H * x->S * (1 + x->prm.iterations);
+        };
+        std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+            if (b->level[x] != b->level[y]) return b->level[x] < b->level[y];
+            return work(x) > work(y);
         });
         double load[pm_batch::kBranches] = {};
+        std::vector<int> branch_of(b->reqs.size(), -1);
         const int nb = std::min<int>(pm_batch::kBranches, (int)order.size());
         PM_CUDA(ctx, cudaEventRecord(b->fork, st));
         for (int k = 0; k < nb; ++k) PM_CUDA(ctx, cudaStreamWaitEvent(b->branch[k], b->fork, 0));
-        for (pm_request *r : order) {
+        for (int idx : order) {
+            pm_request *r = b->reqs[idx];
+            const int pi = r->prior ? batch_index(b, r->prior) : -1;
             int k = 0;
-            for (int q = 1; q < nb; ++q)
-                if (load[q] < load[k]) k = q;
-            load[k] += (double)r->W * r->H * r->S * (1 + r->prm.iterations);
+            if (pi >= 0) {
+                k = branch_of[pi];
+            } else {
+                for (int q = 1; q < nb; ++q)
+                    if (load[q] < load[k]) k = q;
+            }
+            branch_of[idx] = k;
+            load[k] += work(idx);
             const cudaStream_t bs = b->branch[k];
             const pm_params &p = r->prm;
             pm::launch_init_planes(bs, r->trig.row, r->trig.col, r->W, r->H, p.seed, p.keyframe_id, p.init_mode,
@@ -145,6 +204,10 @@ int batch_enqueue(pm_batch *b) {
             ++launches;
             const int kind = pm::image_kind(p.image_format, p.sampler);
             for (int ph = 0; ph < 2 + 2 * p.iterations; ++ph) {
+                if (ph == 2) {
+                    const int rc = seed_in_batch(b, r, bs, launches);
+                    if (rc) return rc;
+                }
                 pm::SweepArgs a = r->args;
                 a.mode = ph < 2 ? pm::kModeScore : pm::kModeSweep;
                 a.colour = ph < 2 ? ph : (ph - 2) & 1;
@@ -158,6 +221,10 @@ int batch_enqueue(pm_batch *b) {
                 if (e != cudaSuccess) return fail(ctx, PM_ECUDA, "tile launch: %s", cudaGetErrorString(e));
                 ++launches;
             }
+            if (p.iterations == 0) {  // no sweep phase: the seeding follows the init scoring
+                const int rc = seed_in_batch(b, r, bs, launches);
+                if (rc) return rc;
+            }
             if (p.postprocess) {
                 enqueue_post(r, bs);
                 launches += 3;
@@ -170,18 +237,29 @@ int batch_enqueue(pm_batch *b) {
         b->launches_per_run = launches;
         return PM_OK;
     }
-    for (pm_request *r : b->reqs) {
+    for (int lv = 0; lv < b->n_levels; ++lv) {
+    for (size_t k = 0; k < b->reqs.size(); ++k) {
+        if (b->level[k] != lv) continue;
+        pm_request *r = b->reqs[k];
         const pm_params &p = r->prm;
         pm::launch_init_planes(st, r->trig.row, r->trig.col, r->W, r->H, p.seed, p.keyframe_id, p.init_mode,
                                p.min_depth, p.max_depth, r->plane, r->score, r->best);
         ++launches;
     }
     for (int ph = 0; ph < max_phases; ++ph) {
+        if (ph == 2) {
+            // seeding of this level's requests, between the init scoring and the sweeps
+            for (size_t k = 0; k < b->reqs.size(); ++k) {
+                if (b->level[k] != lv) continue;
+                const int rc = seed_in_batch(b, b->reqs[k], st, launches);
+                if (rc) return rc;
+            }
+        }
         const int mode = ph < 2 ? pm::kModeScore : pm::kModeSweep;
         const int colour = ph < 2 ? ph : (ph - 2) & 1;
         const int sweep = ph < 2 ? 0 : (ph - 2) >> 1;
         for (auto &g : b->groups) {
-            if (ph >= g.n_phases) continue;
+            if (g.level != lv || ph >= g.n_phases) continue;
             if (b->executor == PM_BATCH_PERSISTENT || b->executor == PM_BATCH_MIXED) {
                 pm::BatchArgs a{};
                 a.args = g.d_args;
@@ -217,11 +295,18 @@ int batch_enqueue(pm_batch *b) {
             }
         }
     }
-    for (pm_request *r : b->reqs)
-        if (r->prm.postprocess) {
-            enqueue_post(r, st);
+    if (max_phases <= 2)  // no sweep phase in the batch: the seeding follows the init scoring
+        for (size_t k = 0; k < b->reqs.size(); ++k) {
+            if (b->level[k] != lv) continue;
+            const int rc = seed_in_batch(b, b->reqs[k], st, launches);
+            if (rc) return rc;
+        }
+    for (size_t k = 0; k < b->reqs.size(); ++k)
+        if (b->level[k] == lv && b->reqs[k]->prm.postprocess) {
+            enqueue_post(b->reqs[k], st);
             launches += 3;
         }
+    }  // level
     b->launches_per_run = launches;
     return PM_OK;
 }
@@ -295,11 +380,11 @@ int pm_batch_run(pm_batch *b) {
     pm_ctx *ctx = b->ctx;
     NvtxRange range("pm_batch_run requests=%d", (int)b->reqs.size());
     if (b->reqs.empty()) return fail(ctx, PM_EINVAL, "empty batch");
+    bool seeded = false;
     for (pm_request *r : b->reqs) {
         int rc = check_views(r);
         if (rc) return rc;
-        if (r->prior || r->prior_res || r->n_lm > 0)
-            return fail(ctx, PM_EINVAL, "batched requests are not seeded (clear the prior and landmarks)");
+        seeded = seeded || r->prior || r->prior_res || r->n_lm > 0;
     }
     // the graph bakes in each request's shape, parameters and mask use
     std::vector<char> sig;
@@ -313,10 +398,25 @@ int pm_batch_run(pm_batch *b) {
         sig.insert(sig.end(), p2, p2 + sizeof r->prm);
     }
     for (pm_request *r : b->reqs) fill_args(r);
-    if (b->executor == PM_BATCH_LAUNCHES || b->executor == PM_BATCH_STREAMS)  // launches bake the poses in
+    // launches bake the poses in; so do the seeding launches (prior pose, landmark count)
+    if (seeded || b->executor == PM_BATCH_LAUNCHES || b->executor == PM_BATCH_STREAMS)
         for (pm_request *r : b->reqs) {
             const char *p3 = reinterpret_cast<const char *>(&r->args);
             sig.insert(sig.end(), p3, p3 + sizeof r->args);
+            const void *links[3] = {r->prior, r->prior_res, r->lm};
+            const char *p4 = reinterpret_cast<const char *>(links);
+            sig.insert(sig.end(), p4, p4 + sizeof links);
+            const int nlm = r->n_lm;
+            const char *p5 = reinterpret_cast<const char *>(&nlm);
+            sig.insert(sig.end(), p5, p5 + sizeof nlm);
+            if (r->prior) {
+                const char *p6 = reinterpret_cast<const char *>(r->prior->R[0]);
+                sig.insert(sig.end(), p6, p6 + sizeof(double) * 12);
+            }
+            if (r->prior_res) {
+                const char *p7 = reinterpret_cast<const char *>(r->prior_res->R);
+                sig.insert(sig.end(), p7, p7 + sizeof(double) * 12);
+            }
         }
     const int ex[2] = {b->executor, b->grid_mult};
     sig.insert(sig.end(), reinterpret_cast<const char *>(ex), reinterpret_cast<const char *>(ex) + sizeof ex);
@@ -346,10 +446,16 @@ int pm_batch_run(pm_batch *b) {
         b->dirty = false;
         b->signature = sig;
     }
-    // the requests' own streams carry their uploads; the batch waits for them
+    // the requests' own streams carry their uploads; the batch waits for them,
+    // and for the priors from outside the batch
     for (size_t k = 0; k < b->reqs.size(); ++k) {
         PM_CUDA(ctx, cudaEventRecord(b->req_events[k], b->reqs[k]->stream));
         PM_CUDA(ctx, cudaStreamWaitEvent(b->stream, b->req_events[k], 0));
+        pm_request *r = b->reqs[k];
+        if ((r->prior && batch_index(b, r->prior) < 0) || r->prior_res) {
+            const int rc = pmi::wait_prior_ready(r, b->stream);
+            if (rc) return rc;
+        }
     }
     // per-request arguments (poses may have changed since the graph was built)
     for (auto &g : b->groups) {

@@ -141,6 +141,14 @@ PM_INTERNAL int enqueue_post(pm_request *r, cudaStream_t st = nullptr);
 // on `st`, with the band counters reset there first; *out is null when the
 // request runs one CTA per tile.
 PM_INTERNAL int tile_band(pm_request *r, dim3 grid, cudaStream_t st, pm::BandArgs *band, const pm::BandArgs **out);
+// Enqueue r's seeding on st: landmark seeds, then its prior request or
+// retained result (the stage of pm_request_run between the init scoring and
+// the sweeps).  in_batch: the prior is a request of the same batch whose
+// post-filter is enqueued earlier on that batch's streams.
+PM_INTERNAL int enqueue_seeding(pm_request *r, cudaStream_t st, bool in_batch);
+// Order st after the work that produces r's prior (a request's stream up to
+// now, or a retained result's snapshot).
+PM_INTERNAL int wait_prior_ready(pm_request *r, cudaStream_t st);
 // Replace the prior links of r (request or retained result, at most one set),
 // keeping the priors' dependent lists in step.
 PM_INTERNAL void link_prior(pm_request *r, const pm_request *prior, const pm_result *res);

@@ -69,14 +69,79 @@ def test_batch_equals_individual_runs(ctx, batch_requests):
         r.close()
 
 
-def test_batch_rejects_seeded_requests(ctx, batch_requests):
+def _landmarks(view, W, H, n, rng):
+    i = rng.integers(8, H - 8, n)
+    j = rng.integers(8, W - 8, n)
+    d = view.depth[i, j].astype(np.float64)
+    lat = -np.pi * (i / H - 0.5)
+    lon = 2 * np.pi * (j / W - 0.5)
+    b = np.stack([np.cos(lat) * np.sin(lon), -np.sin(lat), np.cos(lat) * np.cos(lon)], 1)
+    return (b * d[:, None] - view.t[None]) @ view.R
+
+
+def test_seeded_batch_equals_individual_runs(ctx):
+    """Seeded requests in a batch: a coarse-to-fine chain (the full-size
+    request seeded from a half-size request of the same batch), a request
+    seeded from SLAM landmarks, one from a retained result and one from a
+    request outside the batch.  Every executor gives the maps of the same
+    requests run one at a time in dependency order, bit for bit."""
+    sc = scene.Scene(scene.ROOM_OBJECTS, 44)
+    R, t = sc.poses(4, 44, 0.2, 0.5, 15.0)
+    full = [sc.render(R[k], t[k], 512, 256) for k in range(4)]
+    half = [sc.render(R[k], t[k], 256, 128) for k in range(4)]
+    other = scene.make_request(scene.ROOM_OBJECTS, 384, 192, 3, seed=45)
+
+    def req(W, H, views, Rs, ts, it, kf):
+        r = ctx.request(W, H, len(views) - 1, native.default_params(iterations=it, keyframe_id=kf, seed=kf))
+        r.set_views([v.gray_u8 for v in views], Rs, ts)
+        return r
+
+    coarse = req(256, 128, half, R, t, 6, 1)
+    fine = req(512, 256, full, R, t, 2, 2)
+    fine.set_prior(coarse)
+    lmk = req(512, 256, full, R, t, 2, 3)
+    lmk.set_landmarks(_landmarks(full[0], 512, 256, 300, np.random.default_rng(1)))
+    outside = req(384, 192, other.views, other.R, other.t, 3, 4)
+    from_req = req(384, 192, other.views, other.R, other.t, 2, 5)
+    from_req.set_prior(outside)
+    res = native.Result(ctx, 384, 192)
+    from_res = req(384, 192, other.views, other.R, other.t, 2, 6)
+    from_res.set_prior(res)
+    plain = req(256, 128, half, R, t, 3, 7)
+    outside.run()
+    res.snapshot(outside)
+    outside.synchronize()
+    batch = [coarse, fine, lmk, from_req, from_res, plain]
+    alone = []
+    for r in batch:  # dependency order: the coarse pass before the fine one
+        r.run()
+        r.synchronize()
+        alone.append(r.read(raw=True, want=("depth", "score", "plane")))
+    b = native.Batch(ctx, batch)
+    for executor, mult in ((native.BATCH_PERSISTENT, 1), (native.BATCH_LAUNCHES, 1), (native.BATCH_STREAMS, 1),
+                           (native.BATCH_MIXED, 1)):
+        b.set_executor(executor, mult)
+        b.run()
+        b.synchronize()
+        for r, a in zip(batch, alone):
+            got = r.read(raw=True, want=("depth", "score", "plane"))
+            for k in ("depth", "score", "plane"):
+                assert np.array_equal(got[k], a[k]), (executor, k, r.W, r.S)
+    b.close()
+    for r in batch + [outside]:
+        r.close()
+    res.close()
+
+
+def test_batch_rejects_a_cycle_of_priors(ctx, batch_requests):
     rs = _make(ctx, batch_requests[:2])
-    rs[0].run()
+    rs[0].set_prior(rs[1])
     rs[1].set_prior(rs[0])
     b = native.Batch(ctx, rs)
     with pytest.raises(native.PmError) as e:
         b.run()
     assert e.value.status == native.PM_EINVAL
+    rs[0].set_prior(None)
     rs[1].set_prior(None)
     b.run()
     b.synchronize()
