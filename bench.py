@@ -58,6 +58,7 @@ WORKLOAD = ("plain PatchMatch, one 1920x960 u8 equirect keyframe + 6 sources per
             "(1 px round trip, 0.01 relative depth, 3 of 5 views) and point fusion (0.08) against 4 resident "
             "neighbour depth maps, room + 5 boxes + cylinder scene")
 TOP_K = 3
+CHAIN_FINE_SWEEPS = 2  # full-size sweeps of a coarse-to-fine chain (seeded from its half-size pass)
 CLEAN_THR, CLEAN_PX, CLEAN_MIN = 0.01, 1.0, 3
 FUSE_THR = 0.08
 FLOP_PER_SAMPLE = 40  # algorithmic FP32 work of one (pixel, hypothesis, source, tap) sample
@@ -291,7 +292,8 @@ def _stream_quality(res, stream):
 
 def _drive(native, ctx, stream, cfg, realtime: bool):
     """Submit a keyframe stream to a fresh server (at the arrival times when
-    realtime, else all at once) and collect every result."""
+    realtime, else all at once) and collect every result; with dense output,
+    end the stream and collect the fused outputs too (statuses, point counts)."""
     srv = native.Server(ctx, cfg)
     t0 = time.perf_counter()
     tks = []
@@ -303,8 +305,15 @@ def _drive(native, ctx, stream, cfg, realtime: bool):
         tks.append(srv.submit(kf.gray_u8, kf.R, kf.t))
     res = [srv.wait(tk) for tk in tks]
     wall = time.perf_counter() - t0
+    dense = None
+    if cfg.dense_output:
+        srv.finish()
+        dense = []
+        for tk in tks:
+            st, _, xyz, _ = srv.wait_dense(tk)
+            dense.append((st, 0 if xyz is None else len(xyz)))
     srv.close()
-    return res, wall
+    return res, wall, dense
 
 
 def run_served(native, scene, ctx, local: int, args) -> dict:
@@ -314,29 +323,39 @@ def run_served(native, scene, ctx, local: int, args) -> dict:
     base = dict(cache_capacity=40, min_sources=4, max_sources=8, min_baseline=0.05, max_baseline=3.0)
     p8 = native.default_params(iterations=SWEEPS)
     plain_cfg = native.server_config(params=p8, max_inflight=1, seed_from_prior=0, coarse_to_fine=0, **base)
+    overlap_cfg = native.server_config(params=p8, max_inflight=4, seed_from_prior=0, coarse_to_fine=0, **base)
     served_cfg = native.server_config(params=p8, max_inflight=4, seed_from_prior=1, seeded_iterations=2,
                                       prior_lag=4, **base)
     out = {}
-    for name, cfg in (("plain", plain_cfg), ("served", served_cfg)):
+    for name, cfg in (("plain", plain_cfg), ("served_8_sweeps", overlap_cfg), ("served", served_cfg)):
         l0 = ctx.launches
         with ClockSampler(local) as clk:
-            res, wall = _drive(native, ctx, stream, cfg, realtime=False)
+            res, wall, _ = _drive(native, ctx, stream, cfg, realtime=False)
         work = sum(kf.shape[0] * kf.shape[1] * info["n_sources"] for (rc, _, _, info), kf in zip(res, stream)
                    if rc == 0) / 1e6
         accs, valid = _stream_quality(res, stream)
         out[name] = {"value": work / wall, "wall_s": wall, "keyframes": len(stream),
                      "densified": sum(r[0] == 0 for r in res),
+                     "not_densified_too_few_neighbours": sum(r[0] == native.PM_ENOTREADY for r in res),
                      "seeded": sum(r[3]["seeded"] == 1 for r in res if r[0] == 0),
                      "coarse_to_fine": sum(r[3]["seeded"] == 2 for r in res if r[0] == 0),
                      "within_1pct_of_truth": float(np.mean(accs)) if accs else 0.0,
                      "valid_fraction": float(np.mean(valid)) if valid else 0.0,
                      "gpu_launches": int(ctx.launches - l0), "clocks": clk.summary()}
     out["ratio_served_over_plain"] = out["served"]["value"] / out["plain"]["value"]
+    out["ratio_overlap_only_at_8_sweeps"] = out["served_8_sweeps"]["value"] / out["plain"]["value"]
+    out["gain_note"] = ("served_8_sweeps: continuous batching alone, every keyframe 8 full sweeps from a random "
+                        "start; served: the same plus prior results reused as initialisation (2 sweeps when seeded, "
+                        "coarse to fine when no prior exists) - its gain over plain comes mainly from that "
+                        "work reduction, at higher accuracy against the truth (within_1pct_of_truth); all forms "
+                        "count every densified keyframe as (W*H/1e6)*sources")
     sizes = sorted({kf.shape for kf in stream})
     out["stream"] = (f"hall of boxes, 60 s trajectory through 20 waypoints, Poisson {args.served_rate:g} Hz "
                      f"arrivals over the first {args.served_seconds:g} s, sizes {[f'{w}x{h}' for h, w in sizes]} "
                      f"(3:1), 4-8 neighbours within 0.05-3 m from a 40-keyframe device cache; submitted at once")
-    out["forms"] = {"plain": "max_inflight 1, no prior, 8 sweeps", "served": "max_inflight 4, prior result "
+    out["forms"] = {"plain": "max_inflight 1, no prior, 8 sweeps",
+                    "served_8_sweeps": "max_inflight 4, no prior, no coarse-to-fine, 8 sweeps",
+                    "served": "max_inflight 4, prior result "
                     "reused as initialisation (lag 4), 2 sweeps when seeded; a keyframe without a prior runs "
                     "8 sweeps at half resolution, then 2 at full resolution seeded from them"}
 
@@ -345,9 +364,9 @@ def run_served(native, scene, ctx, local: int, args) -> dict:
                                   t_end=args.latency_seconds, device=local)
     lat_cfg = native.server_config(params=p8, max_inflight=4, seed_from_prior=1, seeded_iterations=2, prior_lag=1,
                                    cache_capacity=40, min_sources=6, max_sources=6, min_baseline=0.05,
-                                   max_baseline=3.0)
+                                   max_baseline=3.0, dense_output=1)
     with ClockSampler(local) as clk:
-        res, wall = _drive(native, ctx, lstream, lat_cfg, realtime=True)
+        res, wall, dense = _drive(native, ctx, lstream, lat_cfg, realtime=True)
     lat_all = [r[3]["latency_ms"] for r in res if r[0] == 0]
     lat_seeded = [r[3]["latency_ms"] for r in res if r[0] == 0 and r[3]["seeded"] == 1]
     accs, valid = _stream_quality(res, lstream)
@@ -356,9 +375,16 @@ def run_served(native, scene, ctx, local: int, args) -> dict:
                       "steady_p50_ms": pct(lat_seeded, 50), "steady_p99_ms": pct(lat_seeded, 99),
                       "keyframes": len(lstream), "densified": len(lat_all), "seeded": len(lat_seeded),
                       "within_1pct_of_truth": float(np.mean(accs)) if accs else 0.0,
+                      "dense_output": {"fused": sum(st == 0 for st, _ in dense),
+                                       "points_per_fused_keyframe": float(np.mean([n for st, n in dense if st == 0]))
+                                       if any(st == 0 for st, _ in dense) else 0.0,
+                                       "not_fused_window_never_filled": sum(st == native.PM_ENOTREADY
+                                                                            for st, _ in dense)},
                       "workload": f"1920x960, 6 neighbours, Poisson 10 Hz for {args.latency_seconds:g} s in real "
                                   "time, each keyframe seeded from the one before it (lag 1), the first coarse to "
-                                  "fine; steady = keyframes seeded from an earlier result",
+                                  "fine; consistency filter (centre of 5, 1 px / 0.01) and fusion (head of 5, "
+                                  "0.08) run on the stream alongside; steady = keyframes seeded from an earlier "
+                                  "result",
                       "clocks": clk.summary()}
     return out
 
@@ -460,11 +486,16 @@ BATCH_SIZES = ((960, 480), (1920, 960), (2880, 1440), (3840, 1920))
 def run_batched(native, scene, ctx, local: int, args) -> dict:
     """Batched form: requests of sizes drawn from BATCH_SIZES with 3-10
     sources (room scenes, per-request seeds), densified one at a time
-    (pm_request_run) and as one batch (pm_batch, executor chosen by
-    pm_batch_tune on the first 16 requests)."""
+    (pm_request_run, 8 sweeps), as one batch (pm_batch, executor chosen by
+    pm_batch_tune on the first 16 requests) and as one batch of coarse-to-fine
+    chains: a request at least 1920 wide becomes a half-size request (8
+    sweeps, images resized on the device) plus the full-size request seeded
+    from it (2 sweeps), both in the batch; smaller ones stay at 8 sweeps.
+    Every form is credited (W*H/1e6)*sources per request; accuracy is the
+    fraction of post-filtered pixels within 1 % of the rendered truth."""
     import torch
     rng = np.random.default_rng(12345)
-    reqs, work = [], 0.0
+    reqs, work, truth, views_dev = [], 0.0, [], []
     dev = torch.device("cuda", local)
     for k in range(args.batched_requests):
         W, H = BATCH_SIZES[rng.integers(len(BATCH_SIZES))]
@@ -472,15 +503,31 @@ def run_batched(native, scene, ctx, local: int, args) -> dict:
         sc = scene.Scene(scene.ROOM, 1000 + k)
         R, t = sc.poses(S + 1, 1000 + k, 0.2, 0.5, 15.0)
         r = ctx.request(W, H, S, native.default_params(iterations=SWEEPS, seed=k, keyframe_id=k))
-        img = torch.empty((H, W), dtype=torch.uint8, device=dev)
+        imgs = []
         for v in range(S + 1):
-            sc.render_device(R[v], t[v], W, H, gray=img, stream=torch.cuda.current_stream(dev).cuda_stream)
+            img = torch.empty((H, W), dtype=torch.uint8, device=dev)
+            dmap = torch.empty((H, W), dtype=torch.float32, device=dev) if v == 0 else None
+            sc.render_device(R[v], t[v], W, H, gray=img, depth=dmap,
+                             stream=torch.cuda.current_stream(dev).cuda_stream)
             torch.cuda.current_stream(dev).synchronize()
             r.set_view(v, img.data_ptr(), R[v], t[v])
             r.synchronize()
+            if v == 0:
+                truth.append(dmap.cpu().numpy())
+            imgs.append(img)
+        views_dev.append((imgs, R, t))
         reqs.append(r)
         work += W * H / 1e6 * S
     torch.cuda.synchronize()
+
+    def accuracy(rs):
+        acc = []
+        for r, gt in zip(rs, truth):
+            d = r.read(want=("depth",))["depth"]
+            m = d > 0
+            acc.append(float((np.abs(d[m] - gt[m]) / gt[m] < 0.01).mean()) if m.any() else 0.0)
+        return float(np.mean(acc))
+
     # plain: one keyframe at a time (each request's graph captured by an untimed run)
     for r in reqs:
         r.run()
@@ -490,6 +537,7 @@ def run_batched(native, scene, ctx, local: int, args) -> dict:
         r.run()
         r.synchronize()
     plain_s = time.perf_counter() - t0
+    plain_acc = accuracy(reqs)
     # batched: executor tuned on a subset, then the whole set in one graph
     sub = native.Batch(ctx, reqs[:16])
     tuning = sub.tune()
@@ -500,35 +548,76 @@ def run_batched(native, scene, ctx, local: int, args) -> dict:
     b.run()
     b.synchronize()
     l1 = ctx.launches
-    stream = torch.cuda.ExternalStream(b.stream_handle)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clk:
-        t1 = time.perf_counter()
-        with torch.cuda.stream(stream):
-            e0.record(stream)
-        b.run()
-        with torch.cuda.stream(stream):
-            e1.record(stream)
-        b.synchronize()
-        batch_wall = time.perf_counter() - t1
-    batch_s = e0.elapsed_time(e1) / 1e3
+
+    def timed(batch):
+        stream = torch.cuda.ExternalStream(batch.stream_handle)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with ClockSampler(local) as clk:
+            t1 = time.perf_counter()
+            with torch.cuda.stream(stream):
+                e0.record(stream)
+            batch.run()
+            with torch.cuda.stream(stream):
+                e1.record(stream)
+            batch.synchronize()
+            wall = time.perf_counter() - t1
+        return e0.elapsed_time(e1) / 1e3, wall, clk.summary()
+
+    batch_s, batch_wall, batch_clk = timed(b)
     b.close()
+    # coarse-to-fine chains in one batch
+    coarse = []
+    for r, (imgs, R, t) in zip(reqs, views_dev):
+        if r.W < 1920:
+            continue
+        c = ctx.request(r.W // 2, r.H // 2, r.S, native.default_params(iterations=SWEEPS, seed=r.params.seed,
+                                                                       keyframe_id=r.params.keyframe_id))
+        for v, img in enumerate(imgs):
+            half = ctx.resize(img, r.W // 2, r.H // 2)
+            torch.cuda.synchronize()
+            c.set_view(v, half.data_ptr(), R[v], t[v])
+            c.synchronize()
+        r.set_params(native.default_params(iterations=CHAIN_FINE_SWEEPS, seed=r.params.seed,
+                                           keyframe_id=r.params.keyframe_id))
+        r.set_prior(c)
+        coarse.append(c)
+    chain = native.Batch(ctx, coarse + reqs)
+    chain.set_executor(tuning["executor"], tuning["grid_mult"])
+    l2 = ctx.launches
+    chain.run()
+    chain.synchronize()
+    l3 = ctx.launches
+    chain_s, chain_wall, chain_clk = timed(chain)
+    chain_acc = accuracy(reqs)
+    chain.close()
     names = {native.BATCH_PERSISTENT: "persistent tile queue", native.BATCH_LAUNCHES: "per-request launches",
              native.BATCH_STREAMS: "parallel graph branches",
              native.BATCH_MIXED: "one persistent tile queue over all source counts"}
     for r in reqs:
+        r.set_prior(None)
         r.close()
+    for c in coarse:
+        c.close()
     return {"requests": len(reqs), "work_mpix_views": work,
-            "plain": {"value": work / plain_s, "seconds": plain_s, "form": "pm_request_run one at a time"},
+            "plain": {"value": work / plain_s, "seconds": plain_s, "form": "pm_request_run one at a time, 8 sweeps",
+                      "within_1pct_of_truth": plain_acc},
             "batched": {"value": work / batch_s, "seconds": batch_s, "wall_s": batch_wall,
                         "executor": names[tuning["executor"]], "grid_mult": tuning["grid_mult"],
-                        "gpu_launches": int(l1 - l0), "clocks": clk.summary()},
+                        "gpu_launches": int(l1 - l0), "clocks": batch_clk,
+                        "form": "one graph, 8 sweeps, maps bit-identical to plain"},
+            "batched_coarse_to_fine": {"value": work / chain_s, "seconds": chain_s, "wall_s": chain_wall,
+                                       "gpu_launches": int(l3 - l2), "clocks": chain_clk,
+                                       "within_1pct_of_truth": chain_acc, "chains": len(coarse),
+                                       "form": f"one graph; requests >= 1920 wide: half size {SWEEPS} sweeps, then "
+                                               f"full size {CHAIN_FINE_SWEEPS} sweeps seeded from it; "
+                                               f"smaller: {SWEEPS} sweeps"},
             "ratio_batched_over_plain": plain_s / batch_s,
+            "ratio_coarse_to_fine_batch_over_plain": plain_s / chain_s,
             "tuning_ms_first16": dict(zip(["persistent x1", "persistent x2", "per-request launches",
                                            "parallel graph branches", "mixed persistent"], tuning["candidate_ms"])),
             "workload": f"{len(reqs)} requests, sizes uniform over {[f'{w}x{h}' for w, h in BATCH_SIZES]}, 3-10 "
-                        f"sources, room scenes with per-request seeds, {SWEEPS} sweeps; results bit-identical "
-                        "between the forms"}
+                        f"sources, room scenes with per-request seeds; the 8-sweep batch is bit-identical to "
+                        "plain, the coarse-to-fine batch does less work at the accuracy shown"}
 
 
 class KeyframeStep:

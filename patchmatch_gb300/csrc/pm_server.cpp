@@ -856,6 +856,28 @@ void dense_step(pm_server *s) {
     dense_retire(s, false);
 }
 
+// Allocate an image size's filter and fusion buffers when its first keyframe
+// is admitted: device and pinned allocations synchronise the device, which
+// would stall keyframes in flight if it happened later in the stream.  A
+// window holds five cleaned maps; one more is produced while the head's
+// fusion results travel to the host, and one is being cleaned.
+constexpr int kDenseMaps = 8;
+void dense_prepare(pm_server *s, int W, int H) {
+    if (!s->cfg.dense_output) return;
+    for (auto &w : s->windows)
+        if (w->W == W && w->H == H) return;
+    SizeWindows *w = windows_for(s, W, H);
+    slot_alloc(*w);  // a failure shows again at the first fusion
+    for (int k = 0; k < kDenseMaps; ++k) {
+        float *d = nullptr;
+        if (cudaMalloc(&d, (size_t)W * H * sizeof(float)) != cudaSuccess) {
+            cudaGetLastError();
+            break;  // take_map allocates later, as needed
+        }
+        w->free_maps.push_back(d);
+    }
+}
+
 bool dense_busy(const pm_server *s) {
     for (const auto &w : s->windows)
         if (w->slot.stage != 0) return true;
@@ -950,6 +972,7 @@ void worker_main(pm_server *s) {
             }
             // admission happens in submission order, so the cache holds exactly
             // the keyframes before this one: neighbours never depend on timing
+            dense_prepare(s, sub.W, sub.H);
             CachedKeyframe *kf = nullptr;
             int rc = cache_insert(s, sub, &kf);
             if (!rc) {
