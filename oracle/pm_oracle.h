@@ -20,9 +20,11 @@
  *
  * Parity status: pinned against outputs of the reference's own CUDA kernels,
  * compiled unmodified from its sources and run on a GB300 (fixtures under
- * tests/golden/, generated by tests/golden/make_golden.py).  The reference's
- * C++ CPU path needs OpenCV and cannot be compiled here; its arithmetic is
- * restated directly instead.
+ * tests/golden/, generated by tests/golden/make_golden.py), and against the
+ * reference's own host stages (PostProcess, DepthmapCleaner::Clean,
+ * DepthmapPruner::Prune of depthmap.cc, compiled unmodified against a
+ * minimal OpenCV stand-in by oracle/refhost.py; fixtures from
+ * tests/golden/make_golden_host.py): bit-exact.
  *
  * Random numbers: the reference seeds cuRAND XORWOW from clock64() and is not
  * reproducible.  This restatement (and the product) instead draws from

@@ -122,3 +122,27 @@ def test_chain_from_resident_requests(ctx):
     assert (got > 0).mean() > 0.15  # 4 sweeps, 2 sources, 1 % agreement of 3 of 5 views
     for r in reqs:
         r.close()
+
+
+def test_gpu_filter_and_fuse_equal_reference_host_golden(ctx):
+    """The GPU consistency filter and fusion against the reference's own
+    host Clean and Prune (golden fixture of depthmap.cc compiled unmodified):
+    keep decisions equal, kept depths and pixel indices identical."""
+    import os
+    fix = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_host_96x48.npz")
+    if not os.path.exists(fix):
+        pytest.skip("golden fixture not generated")
+    gold = dict(np.load(fix))
+    for case in (0, 1):
+        d = list(gold[f"c{case}_depths"])
+        R, t = gold[f"c{case}_R"], gold[f"c{case}_t"]
+        thr_c, thr_p = (float(x) for x in gold[f"c{case}_thr"])
+        g = ctx.filter_consistency(d, R, t, center=2, thr=thr_c, min_consistent=3)
+        ref = gold[f"c{case}_clean"]
+        assert ((g > 0) == (ref > 0)).mean() >= 0.999, case
+        both = (g > 0) & (ref > 0)
+        assert np.array_equal(g[both], ref[both])
+        pruned, xyz, cols, ij, _ = ctx.fuse(d, R, t, gold[f"c{case}_bgr"], thr_p)
+        assert ((pruned > 0) == (gold[f"c{case}_pruned"] > 0)).mean() >= 0.999, case
+        common = np.intersect1d(ij[:, 0] * 96 + ij[:, 1], gold[f"c{case}_ij"][:, 0] * 96 + gold[f"c{case}_ij"][:, 1])
+        assert len(common) >= 0.999 * max(len(ij), len(gold[f"c{case}_ij"]))
