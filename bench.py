@@ -488,9 +488,12 @@ def run_batched(native, scene, ctx, local: int, args) -> dict:
     sources (room scenes, per-request seeds), densified one at a time
     (pm_request_run, 8 sweeps), as one batch (pm_batch, executor chosen by
     pm_batch_tune on the first 16 requests) and as one batch of coarse-to-fine
-    chains: a request at least 1920 wide becomes a half-size request (8
-    sweeps, images resized on the device) plus the full-size request seeded
-    from it (2 sweeps), both in the batch; smaller ones stay at 8 sweeps.
+    chains: a request 1920 wide becomes a half-size request (8 sweeps, images
+    resized on the device) plus the full-size request seeded from it (2
+    sweeps); wider ones a quarter-size (8), half-size (2) and full-size (2)
+    chain; 960 wide ones stay at 8 sweeps.  Measured per request at 6 sources:
+    these chains keep the post-filtered coverage and reach at least plain's
+    accuracy, while a single full-size sweep loses a fifth of the coverage.
     Every form is credited (W*H/1e6)*sources per request; accuracy is the
     fraction of post-filtered pixels within 1 % of the rendered truth."""
     import torch
@@ -565,22 +568,30 @@ def run_batched(native, scene, ctx, local: int, args) -> dict:
 
     batch_s, batch_wall, batch_clk = timed(b)
     b.close()
-    # coarse-to-fine chains in one batch
+    # coarse-to-fine chains in one batch: 1920 wide: half size (8 sweeps) then
+    # full size (2); wider: quarter size (8), half (2), full (2)
     coarse = []
     for r, (imgs, R, t) in zip(reqs, views_dev):
         if r.W < 1920:
             continue
-        c = ctx.request(r.W // 2, r.H // 2, r.S, native.default_params(iterations=SWEEPS, seed=r.params.seed,
-                                                                       keyframe_id=r.params.keyframe_id))
-        for v, img in enumerate(imgs):
-            half = ctx.resize(img, r.W // 2, r.H // 2)
-            torch.cuda.synchronize()
-            c.set_view(v, half.data_ptr(), R[v], t[v])
-            c.synchronize()
+        levels = [4, 2] if r.W >= 2880 else [2]
+        prev = None
+        for lv, f in enumerate(levels):
+            c = ctx.request(r.W // f, r.H // f, r.S,
+                            native.default_params(iterations=SWEEPS if lv == 0 else CHAIN_FINE_SWEEPS,
+                                                  seed=r.params.seed, keyframe_id=r.params.keyframe_id))
+            for v, img in enumerate(imgs):
+                small = ctx.resize(img, r.W // f, r.H // f)
+                torch.cuda.synchronize()
+                c.set_view(v, small.data_ptr(), R[v], t[v])
+                c.synchronize()
+            if prev is not None:
+                c.set_prior(prev)
+            coarse.append(c)
+            prev = c
         r.set_params(native.default_params(iterations=CHAIN_FINE_SWEEPS, seed=r.params.seed,
                                            keyframe_id=r.params.keyframe_id))
-        r.set_prior(c)
-        coarse.append(c)
+        r.set_prior(prev)
     chain = native.Batch(ctx, coarse + reqs)
     chain.set_executor(tuning["executor"], tuning["grid_mult"])
     l2 = ctx.launches
@@ -597,6 +608,8 @@ def run_batched(native, scene, ctx, local: int, args) -> dict:
         r.set_prior(None)
         r.close()
     for c in coarse:
+        c.set_prior(None)
+    for c in coarse:
         c.close()
     return {"requests": len(reqs), "work_mpix_views": work,
             "plain": {"value": work / plain_s, "seconds": plain_s, "form": "pm_request_run one at a time, 8 sweeps",
@@ -607,10 +620,11 @@ def run_batched(native, scene, ctx, local: int, args) -> dict:
                         "form": "one graph, 8 sweeps, maps bit-identical to plain"},
             "batched_coarse_to_fine": {"value": work / chain_s, "seconds": chain_s, "wall_s": chain_wall,
                                        "gpu_launches": int(l3 - l2), "clocks": chain_clk,
-                                       "within_1pct_of_truth": chain_acc, "chains": len(coarse),
-                                       "form": f"one graph; requests >= 1920 wide: half size {SWEEPS} sweeps, then "
-                                               f"full size {CHAIN_FINE_SWEEPS} sweeps seeded from it; "
-                                               f"smaller: {SWEEPS} sweeps"},
+                                       "within_1pct_of_truth": chain_acc, "coarse_requests": len(coarse),
+                                       "form": f"one graph; 1920 wide: half size {SWEEPS} sweeps, then full size "
+                                               f"{CHAIN_FINE_SWEEPS} seeded from it; 2880 and 3840 wide: quarter "
+                                               f"size {SWEEPS}, half {CHAIN_FINE_SWEEPS}, full {CHAIN_FINE_SWEEPS}, "
+                                               f"each seeded from the one before; 960 wide: {SWEEPS} sweeps"},
             "ratio_batched_over_plain": plain_s / batch_s,
             "ratio_coarse_to_fine_batch_over_plain": plain_s / chain_s,
             "tuning_ms_first16": dict(zip(["persistent x1", "persistent x2", "per-request launches",
