@@ -27,7 +27,7 @@ __device__ __forceinline__ void visit(const SweepArgs &sa, int bx, int by, float
 }
 
 template <bool Plain>
-__global__ void __launch_bounds__(kThreads, 2) batch_mixed_kernel(const __grid_constant__ BatchArgs b) {
+__global__ void __launch_bounds__(kThreads, 2 * kCtaScale) batch_mixed_kernel(const __grid_constant__ BatchArgs b) {
     extern __shared__ float4 tile[];
     __shared__ SweepArgs sa;
     __shared__ int s_item;

@@ -19,9 +19,13 @@
 
 namespace pm {
 
+#ifndef PM_TILE_H
+#define PM_TILE_H 8
+#endif
 constexpr int kTileW = 64;
-constexpr int kTileH = 8;
+constexpr int kTileH = PM_TILE_H;  // rows per tile = warps per CTA
 constexpr int kThreads = kTileH * 32;
+constexpr int kCtaScale = 8 / kTileH;  // CTAs per SM scale inversely with the CTA size
 constexpr int kHaloMax = 5;                       // largest supported patch_half
 constexpr int kTileRows = kTileH + 2 * kHaloMax;  // 18
 constexpr int kTileCols = (kTileW + 2 * kHaloMax) / 2;  // 37 same-colour entries per row
@@ -88,7 +92,9 @@ __host__ __device__ constexpr size_t tile_kernel_smem_max() {
                : tile_kernel_smem<PM_FACTOR_MAX_SOURCES>();
 }
 // Three CTAs of the largest layout fit one SM's 228 KB of shared memory.
-static_assert(3 * (tile_kernel_smem_max() + 1024) <= 228 * 1024, "tile layout exceeds the per-SM shared memory");
+static_assert(3 * kCtaScale * (tile_kernel_smem<8>() + 1024) <= 228 * 1024 &&
+                  2 * kCtaScale * (tile_kernel_smem_max() + 1024) <= 228 * 1024,
+              "tile layout exceeds the per-SM shared memory");
 
 // Ask for the smallest shared-memory carveout that holds `blocks` CTAs of
 // `kernel` with `dyn` bytes of dynamic shared memory, leaving the rest of the
@@ -184,9 +190,9 @@ struct Park {
 // 3 % faster; 5-6 sources spill and run 1-3 % slower).  The persistent
 // kernels (banded, batched) keep 3: at 64 registers they spill.
 template <int S>
-constexpr int persistent_min_blocks() { return S <= 8 ? 3 : 2; }
+constexpr int persistent_min_blocks() { return (S <= 8 ? 3 : 2) * kCtaScale; }
 template <int S>
-constexpr int tile_min_blocks() { return S <= 4 ? 4 : persistent_min_blocks<S>(); }
+constexpr int tile_min_blocks() { return S <= 4 ? 4 * kCtaScale : persistent_min_blocks<S>(); }
 
 // Smoothness factor f in [0, 1] of a propagated plane p against the pixel's
 // current plane h and its depth before propagation (PatchMatchCuda.cu:322-337).
