@@ -29,14 +29,16 @@ def build(force: bool = False):
         return None
     src = os.path.join(HERE, "ref_host_harness.cc")
     shim = os.path.join(HERE, "refshim_host", "opencv2", "opencv.hpp")
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(src),
-                                                                          os.path.getmtime(shim)):
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(
+            os.path.getmtime(src), os.path.getmtime(shim), os.path.getmtime(os.path.abspath(__file__))):
         return LIB
     os.makedirs(os.path.dirname(LIB), exist_ok=True)
     subprocess.check_call(["g++", "-std=c++17", "-O2", "-fopenmp", "-fPIC", "-shared",
                            "-I" + os.path.join(HERE, "refshim_host"), "-I" + os.path.join(CUDA, "include"),
                            "-I" + os.path.dirname(REFERENCE_CC), src, REFERENCE_CC, "-o", LIB,
-                           "-L" + os.path.join(CUDA, "lib64"), "-lcudart"],
+                           # the package library, loaded RTLD_GLOBAL, exports the same dense::
+                           # class names (it mirrors this interface): bind to our own copies
+                           "-Wl,-Bsymbolic", "-L" + os.path.join(CUDA, "lib64"), "-lcudart"],
                           stdout=subprocess.DEVNULL, stderr=subprocess.STDOUT)
     return LIB
 
