@@ -171,8 +171,8 @@ def _hbm_view(traffic, launch_ms):
 # (dram__bytes_read.sum + dram__bytes_write.sum), valid only for the kernel
 # sources it was measured on: a different build reports null rather than a
 # stale figure.
-TRAFFIC_NCU = {"bytes_per_launch": 59448576,
-               "sources_sha256": "c7a3276da8edf9b036782efc1e51b8ca00dd52504207c4caca10722aa50f4121"}
+TRAFFIC_NCU = {"bytes_per_launch": 59172096,
+               "sources_sha256": "f127616ae86226543b4dc35890b1d4e8dca306ee5bc5c24bbe3903428dfc70ea"}
 KERNEL_SOURCES = ("patchmatch_gb300/csrc/pm_sweep.cuh", "patchmatch_gb300/csrc/pm_device.cuh",
                   "patchmatch_gb300/csrc/pm_inst.cu", "patchmatch_gb300/csrc/pm_types.h")
 
