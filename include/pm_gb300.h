@@ -414,10 +414,11 @@ int pm_server_wait(pm_server *srv, uint64_t ticket, int timeout_ms, pm_maps *out
 /* With dense_output: blocks until the ticket's fused output exists (timeout as
  * pm_server_wait), then fills depth (H x W host floats: the keyframe's depth
  * after the consistency filter and fusion, may be NULL) and points (host:
- * xyz world FP64 and ij (row, col) of the points fusion kept, up to
- * points->capacity; points->count receives the total, PM_EINVAL when it
- * exceeds the capacity; bgr is not written, the served loop receives gray
- * images).  Returns PM_OK, PM_ENOTREADY for a keyframe that was not densified
+ * xyz world FP64 and ij (row, col) of the points fusion kept;
+ * points->count receives their number.  When it exceeds points->capacity
+ * nothing is written, the call returns PM_EINVAL with points->count set and
+ * the ticket stays collectable with a larger buffer; bgr is not written, the
+ * served loop receives gray images).  Returns PM_OK, PM_ENOTREADY for a keyframe that was not densified
  * or whose filter or fusion window never filled (the first two and the last
  * keyframes of each image size, as in the reference), PM_ECANCELLED for one
  * cancelled by pm_server_destroy, or PM_EINVAL (no dense output, unknown or
@@ -426,7 +427,8 @@ int pm_server_wait_dense(pm_server *srv, uint64_t ticket, int timeout_ms, float 
 /* End of the stream: refuses further submissions (PM_ECANCELLED), densifies
  * every keyframe already submitted, completes every dense output (those whose
  * windows never filled with PM_ENOTREADY) and returns when all results exist;
- * they stay collectable until pm_server_destroy. */
+ * they stay collectable until pm_server_destroy.  A pm_server_destroy on
+ * another thread while this call blocks returns only after it has. */
 int pm_server_finish(pm_server *srv);
 /* Finishes the keyframes already on the GPU; keyframes still queued complete
  * with PM_ECANCELLED (and their dense outputs too).  Returns once every thread

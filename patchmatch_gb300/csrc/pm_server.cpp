@@ -1147,6 +1147,11 @@ int pm_server_wait_dense(pm_server *s, uint64_t ticket, int timeout_ms, float *d
         else if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), pred))
             return PM_ETIMEOUT;
         if (!s->dense_done.count(ticket)) return PM_EINVAL;
+        const DenseResult &d = s->dense_done[ticket];
+        if (points && d.status == PM_OK && (long long)(d.ij.size() / 2) > (long long)points->capacity) {
+            points->count = (int)(d.ij.size() / 2);  // too small: the ticket stays collectable
+            return PM_EINVAL;
+        }
         r = std::move(s->dense_done[ticket]);
         s->dense_done.erase(ticket);
         s->dense_outstanding.erase(ticket);
@@ -1166,7 +1171,6 @@ int pm_server_wait_dense(pm_server *s, uint64_t ticket, int timeout_ms, float *d
             }
         }
         points->count = n;
-        if (n > points->capacity) return PM_EINVAL;
     }
     return PM_OK;
 }
@@ -1176,6 +1180,7 @@ int pm_server_finish(pm_server *s) {
     std::unique_lock<std::mutex> lk(s->mu);
     s->finishing = true;
     s->cv_work.notify_all();
+    WaiterScope ws(s);  // a concurrent destroy waits until this thread has left
     s->cv_done.wait(lk, [&] { return s->finished; });
     return PM_OK;
 }

@@ -200,3 +200,58 @@ def test_producer_that_never_collects_does_not_block(ctx, views):
     stalled.set()
     th.join()
     srv.close()
+
+
+def test_short_points_buffer_leaves_the_ticket_collectable(ctx, views):
+    """pm_server_wait_dense with a points buffer smaller than the fused cloud
+    returns PM_EINVAL with the count and writes nothing; the same ticket is
+    then collected with a buffer of that size and equals the full-size read
+    of a second, identical server."""
+    import ctypes as C
+    outs, sel = [], None
+    for short in (True, False):
+        srv = native.Server(ctx, _cfg(dense_output=1))
+        tks = [srv.submit(v.gray_u8, v.R, v.t) for v in views]
+        for tk in tks:
+            srv.wait(tk)
+        srv.finish()
+        depth = np.zeros((H, W), np.float32)
+        if short:
+            # the first ticket with a fused cloud (the stream's first keyframes have none)
+            xyz1 = np.full((1, 3), 7.0)
+            ij1 = np.full((1, 2), 7, np.int32)
+            for sel, tk in enumerate(tks):
+                pts = native.Points(1, 0, xyz1.ctypes.data, None, ij1.ctypes.data)
+                rc = srv._L.pm_server_wait_dense(srv.h, tk, -1, depth.ctypes.data, C.byref(pts))
+                if rc != native.PM_ENOTREADY:
+                    break
+            assert rc == native.PM_EINVAL and pts.count > 1
+            assert (xyz1 == 7.0).all() and (ij1 == 7).all() and (depth == 0).all()
+            n = pts.count
+        else:
+            n = H * W
+        tk = tks[sel]
+        xyz = np.zeros((n, 3), np.float64)
+        ij = np.zeros((n, 2), np.int32)
+        pts = native.Points(n, 0, xyz.ctypes.data, None, ij.ctypes.data)
+        assert srv._L.pm_server_wait_dense(srv.h, tk, -1, depth.ctypes.data, C.byref(pts)) == native.PM_OK
+        outs.append((depth.copy(), xyz[:pts.count].copy(), ij[:pts.count].copy()))
+        srv.close()
+    (d0, x0, i0), (d1, x1, i1) = outs
+    assert len(x0) > 1 and np.array_equal(d0, d1) and np.array_equal(i0, i1) and np.array_equal(x0, x1)
+
+
+def test_finish_and_destroy_from_two_threads(ctx, views):
+    """A thread blocked in pm_server_finish while another destroys the server:
+    destroy returns only after finish has, and both succeed."""
+    srv = native.Server(ctx, _cfg(inflight=1, dense_output=1))
+    for v in views[:6]:
+        srv.submit(v.gray_u8, v.R, v.t)
+    got = {}
+    th = threading.Thread(target=lambda: got.setdefault("finish", srv._L.pm_server_finish(srv.h)))
+    th.start()
+    time.sleep(0.05)
+    assert srv._L.pm_server_destroy(srv.h) == native.PM_OK
+    srv.h = None
+    th.join(10.0)
+    assert not th.is_alive() and got["finish"] == native.PM_OK
