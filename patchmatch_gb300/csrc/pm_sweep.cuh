@@ -183,14 +183,18 @@ struct Park {
 };
 
 // Resident CTAs per SM the register allocation targets: 3 (80 registers)
-// holds up to 8 sources with the visit state parked; more sources need the
-// 128-register budget.  The one-CTA-per-tile kernel runs 4 (64 registers, no
-// spills) up to 4 sources, where the extra warps hide more texture latency
-// (measured, 8 sweeps at 1920x960: 2 sources 3 %, 3 sources 1 %, 4 sources
-// 3 % faster; 5-6 sources spill and run 1-3 % slower).  The persistent
-// kernels (banded, batched) keep 3: at 64 registers they spill.
+// up to 7 sources with the visit state parked; from 8 sources 2 (128
+// registers), which also leaves each CTA a larger share of L1 for the
+// texture samples (measured, 8 sweeps, 8 sources: 3840x1920 FP16 banded
+// 444 -> 384 ms, u8 at 960x480 to 3840x1920 1-3 % faster; 7 sources at
+// 1920x960 u8 1 % slower with 2).  The one-CTA-per-tile kernel runs 4 (64
+// registers, no spills) up to 4 sources, where the extra warps hide more
+// texture latency (measured, 8 sweeps at 1920x960: 2 sources 3 %, 3 sources
+// 1 %, 4 sources 3 % faster; 5-6 sources spill and run 1-3 % slower).  The
+// persistent kernels (banded, batched) keep 3 there: at 64 registers they
+// spill.
 template <int S>
-constexpr int persistent_min_blocks() { return (S <= 8 ? 3 : 2) * kCtaScale; }
+constexpr int persistent_min_blocks() { return (S <= 7 ? 3 : 2) * kCtaScale; }
 template <int S>
 constexpr int tile_min_blocks() { return S <= 4 ? 4 * kCtaScale : persistent_min_blocks<S>(); }
 
