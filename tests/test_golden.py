@@ -54,13 +54,13 @@ def test_texture_border_is_clamp(gold):
     assert np.abs(clamp - got).max() < 1.0  # 8-bit texture weights
 
 
-def _replay(gold, interp, combine=O.COMBINE_FOLD):
+def _replay(gold, interp, combine=O.COMBINE_FOLD, arith=O.ARITH_F32_REF):
     imgs = gold["images"].astype(np.float32)
     H, W = imgs[0].shape
     V = O.Views(imgs[0], imgs[1:], gold["R"], gold["t"])
     ii, jj = np.nonzero(_interior(H, W))
     ij = np.stack([ii, jj], 1).astype(np.int32)
-    ours, _ = O.cost_batch(V, O.cost_params(arith=O.ARITH_F32_REF, interp=interp, combine=combine), ij,
+    ours, _ = O.cost_batch(V, O.cost_params(arith=arith, interp=interp, combine=combine), ij,
                            gold["planes"][ii, jj])
     return np.abs(ours - gold["scores"][ii, jj])
 
@@ -68,10 +68,21 @@ def _replay(gold, interp, combine=O.COMBINE_FOLD):
 def test_cost_replays_reference_kernel(gold):
     """ScorePlaneDepth_ on fixed planes: the oracle in the reference's float
     arithmetic, with the texture unit's coordinates rounded to 1/256 texel,
-    reproduces the reference kernel's scores."""
+    reproduces the reference kernel's scores.  The residual is the texture
+    unit's own filter arithmetic, which no host restatement reproduces: even
+    in FP64 the reference kernel's scores are within 1e-5 of the restatement
+    for only a minority of hypotheses (the relative-error floor any
+    comparison against that kernel inherits; the GPU texture sampler, which
+    filters in the same unit, agrees with it far more closely)."""
     err = _replay(gold, O.INTERP_TEX8_RN)
     print(f"tex8-rn: median {np.median(err):.2e} p99 {np.quantile(err, .99):.2e} max {err.max():.2e}")
     assert np.median(err) < 1e-4 and np.quantile(err, 0.99) < 1e-3 and err.max() < 5e-3
+    ref = np.abs(gold["scores"][_interior(*gold["scores"].shape)])
+    e64 = _replay(gold, O.INTERP_TEX8_RN, arith=O.ARITH_F64) / np.maximum(1.0, ref)
+    within = float((e64 <= 1e-5).mean())
+    print(f"reference kernel vs FP64 restatement (1/256 weights): median {np.median(e64):.2e} "
+          f"within 1e-5 {within:.3f}")
+    assert np.median(e64) < 1e-4 and within < 0.5
 
 
 def test_texture_weights_round_to_nearest(gold):
