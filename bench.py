@@ -700,6 +700,99 @@ class KeyframeStep:
         self.nbr = self.work = self.cleaned = self.pruned = self.xyz = self.ij = self.count = self.ws = None
 
 
+def run_precision(native, scene, ctx, local: int) -> dict:
+    """Precision form: one 3840x1920 keyframe with 8 sources as FP16 images
+    (sigma-2 noise on unrounded intensities, FP32 NCC moments), densified at
+    full resolution (8 sweeps) and coarse to fine over its 3-level FP16
+    pyramid (960x480 8 sweeps, 1920x960 and 3840x1920 2 seeded sweeps each),
+    timed with CUDA events on the requests' stream; accuracy against the
+    scene's analytic depth.  The cost error against the FP64 oracle is
+    measured by tests/test_gpu_precision.py."""
+    import torch
+    Wp, Hp, Sp = 3840, 1920, 8
+    dev = torch.device("cuda", local)
+    sc = scene.Scene(scene.ROOM, 77)
+    R, t = sc.poses(Sp + 1, 77, 0.2, 0.5, 15.0)
+    imgs = []
+    for v in range(Sp + 1):
+        g = torch.empty((Hp, Wp), dtype=torch.float32, device=dev)
+        sc.render_device_f32(R[v], t[v], Wp, Hp, g, noise_sigma=2.0, noise_seed=100 + v)
+        imgs.append(g.clamp(0, 255).half())
+    truth = torch.empty((Hp, Wp), dtype=torch.float32, device=dev)
+    sc.render_device(R[0], t[0], Wp, Hp, depth=truth)
+    torch.cuda.synchronize()
+    gt = truth.cpu().numpy()
+    del truth
+
+    def request(views, Wl, Hl, iterations):
+        r = ctx.request(Wl, Hl, Sp, native.default_params(image_format=native.IMAGE_F16, iterations=iterations))
+        for k, im in enumerate(views):
+            r.set_view(k, im.data_ptr(), R[k], t[k])
+        r.synchronize()
+        return r
+
+    def accuracy(r):
+        d = r.read(want=("depth",))["depth"]
+        m = d > 0
+        e = np.abs(d[m] - gt[m]) / gt[m]
+        return {"within_1pct_of_truth": float((e < 0.01).mean()), "median_rel_error": float(np.median(e)),
+                "valid_fraction": float(m.mean())}
+
+    def timed(first, run, reps=3):
+        """ms per run on the last request's stream (all levels run on one stream
+        per request; the chain's levels are ordered by their prior events)."""
+        stream = torch.cuda.ExternalStream(first.stream_handle)
+        run()
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            with torch.cuda.stream(stream):
+                e0.record(stream)
+            last = run()
+            last_stream = torch.cuda.ExternalStream(last.stream_handle)
+            with torch.cuda.stream(last_stream):
+                e1.record(last_stream)
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return float(np.mean(ms))
+
+    full = request(imgs, Wp, Hp, SWEEPS)
+    with ClockSampler(local) as clk:
+        ms_full = timed(full, lambda: (full.run(), full)[1])
+    a_full = accuracy(full)
+    full.close()
+    pyr = [ctx.pyramid_f16(im, 3) for im in imgs]
+    lv2 = request([p[2] for p in pyr], Wp // 4, Hp // 4, SWEEPS)
+    lv1 = request([p[1] for p in pyr], Wp // 2, Hp // 2, CHAIN_FINE_SWEEPS)
+    lv0 = request(imgs, Wp, Hp, CHAIN_FINE_SWEEPS)
+    lv1.set_prior(lv2)
+    lv0.set_prior(lv1)
+
+    def chain():
+        lv2.run()
+        lv1.run()
+        lv0.run()
+        return lv0
+
+    ms_c2f = timed(lv2, chain)
+    a_c2f = accuracy(lv0)
+    for r in (lv0, lv1, lv2):
+        r.close()
+    del pyr, imgs
+    torch.cuda.synchronize()
+    work = Wp * Hp / 1e6 * Sp
+    return {"workload": f"{Wp}x{Hp} FP16 keyframe, {Sp} sources, sigma-2 noise, fold combination, texture "
+                        f"sampler, {SWEEPS} sweeps, post-filter",
+            "full": {"ms": ms_full, "value": work / (ms_full / 1e3), "unit": UNIT, **a_full},
+            "coarse_to_fine": {"ms": ms_c2f, "value": work / (ms_c2f / 1e3), "unit": UNIT,
+                               "levels": f"{Wp // 4}x{Hp // 4} {SWEEPS} sweeps, then {Wp // 2}x{Hp // 2} and "
+                                         f"{Wp}x{Hp} {CHAIN_FINE_SWEEPS} seeded sweeps each", **a_c2f},
+            "clocks": clk.summary(),
+            "cost_error_vs_fp64": "tests/test_gpu_precision.py (1e6 hypotheses x 8 sources)"}
+
+
 def run_ours(args):
     import torch
     rank, ws, local, dist = _dist()
@@ -834,6 +927,7 @@ def run_ours(args):
                   "note": "compare with reference_cuda in the --impl reference line (same scene and sizes)"}
     served = None if args.no_served else run_served(native, scene, ctx, local, args)
     batched = None if args.no_batched else run_batched(native, scene, ctx, local, args)
+    precision = None if args.no_precision else run_precision(native, scene, ctx, local)
     pipeline = run_pipeline(native, scene, ctx, local, args.steps)
     traffic = _traffic()
     # the roofline terms of the cost kernel (samples/s): 40 FP32 flop, 4
@@ -882,6 +976,7 @@ def run_ours(args):
                          "hbm_view": _hbm_view(traffic, sweep_ms)},
             "served": served,
             "batched": batched,
+            "precision": precision,
             "pipeline": pipeline,
             "two_source_sweeps": two_source,
             "cpu_baseline": cpu,
@@ -928,6 +1023,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-served", action="store_true", help="skip the served-form measurement")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-form measurement")
+    ap.add_argument("--no-precision", action="store_true", help="skip the precision-form measurement")
     ap.add_argument("--no-reference-gpu", action="store_true",
                     help="reference arm: skip timing the reference's CUDA path")
     ap.add_argument("--batched-requests", type=int, default=64, help="requests in the batched-form measurement")
