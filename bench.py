@@ -75,6 +75,12 @@ def _samples_per_half_sweep() -> float:
     return interior / 2 * 14 * S * 36
 
 
+def _samples_per_step() -> float:
+    """Algorithmic samples of one keyframe's densification: init scoring (one
+    hypothesis per interior pixel) and 2 x SWEEPS half-sweeps of 14."""
+    return _samples_per_half_sweep() * (2 * SWEEPS + 1 / 7)
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
 
@@ -974,6 +980,11 @@ def run_ours(args):
                          "achieved_samples_per_s": samples_s, "frac_of_binding": samples_s / terms[binding],
                          "probes": {"fp32_tflops": peak, "sfu_gops": sfu, "tex_gfetches": tex},
                          "hbm_view": _hbm_view(traffic, sweep_ms)},
+            "value_vs_roofline": {
+                "samples_per_step": _samples_per_step(),
+                "frac": {k: _samples_per_step() / v / (ms_step / 1e3) for k, v in terms.items()},
+                "note": "the whole step (densification, post-filter, consistency filter, fusion) against the "
+                        "time its algorithmic samples take at each roofline term"},
             "served": served,
             "batched": batched,
             "precision": precision,
