@@ -141,3 +141,42 @@ def test_depth_error_full_resolution_and_coarse_to_fine(ctx, fp16_views):
     assert a_c2f[0] >= a_full[0] and t_c2f < t_full
     for r in (full, lv2, lv1, lv0):
         r.close()
+
+
+@pytest.mark.parametrize("sampler", [native.SAMPLER_EXACT, native.SAMPLER_TEXTURE])
+def test_full_run_band_matches_oracle(ctx, fp16_views, sampler):
+    """The precision workload's full run (3840x1920, 8 FP16 sources, 8
+    sweeps) against the FP64 oracle on the same FP16 values, at the method's
+    tolerance: >= 99 % of the pixels both post-filters keep within 1 %
+    relative depth.  The oracle runs a 120-row band; a half-sweep moves
+    information at most 3 rows (PatchMatchCuda.cu:287-296), so the band's 24
+    central rows see exactly what a full run sees.  The exact sampler is
+    compared with exact bilinear weights, the texture sampler with the
+    oracle's model of the texture unit (1/256 weights)."""
+    R, t, imgs, gt = fp16_views
+    r = _request(ctx, R, t, imgs, W, H, iterations=8, sampler=sampler)
+    r.run()
+    g_raw, g_filt = r.read(raw=True)["depth"], r.read()["depth"]
+    r.close()
+    host = [im.float().cpu().numpy() for im in imgs]
+    reach = 3 * 2 * 8
+    lo, hi = H // 2 - 12 - reach, H // 2 + 12 + reach
+    interp = O.INTERP_EXACT if sampler == native.SAMPLER_EXACT else O.INTERP_TEX8_RN
+    t0 = time.perf_counter()
+    o = O.patchmatch(O.Views(host[0], host[1:], R, t), O.cost_params(interp=interp), iterations=8,
+                     row_lo=lo, row_hi=hi)
+    t_oracle = time.perf_counter() - t0
+    o_filt, _ = O.postprocess(host[0], o["depth"], o["score"])
+    sel = np.zeros((H, W), bool)
+    sel[lo + reach:hi - reach, 6:W - 5] = True
+    both = sel & (g_filt > 0) & (o_filt > 0)
+    agree = float((np.abs(g_filt - o_filt)[both] / o_filt[both] < 0.01).mean())
+    cov_g, cov_o = float((g_filt > 0)[sel].mean()), float((o_filt > 0)[sel].mean())
+    raw = float((np.abs(g_raw - o["depth"]) < 0.01 * o["depth"])[sel].mean())
+    acc = lambda d: float((np.abs(d - gt) / gt < 0.01)[sel & (d > 0)].mean())
+    print(f"FP16 3840x1920x8 band sampler={sampler}: valid-pixel agreement within 1% {agree:.5f} (coverage gpu "
+          f"{cov_g:.4f} oracle {cov_o:.4f}); raw agreement {raw:.5f}; accuracy 1% gpu {acc(g_filt):.4f} oracle "
+          f"{acc(o_filt):.4f}; oracle {t_oracle:.0f} s")
+    assert agree >= 0.99
+    assert cov_g >= cov_o - 0.01
+    assert acc(g_filt) >= acc(o_filt) - 0.01
