@@ -974,7 +974,7 @@ def run_ours(args):
                          "peak_source": "in-run FFMA probe (pm_probe_fp32_peak); MEASURED_PEAKS.json has no FP32 figure",
                          "flop_per_sample": FLOP_PER_SAMPLE, "samples_per_launch": _samples_per_half_sweep(),
                          "launch_ms": sweep_ms, "traffic": traffic,
-                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of this build's "
+                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the current sources' "
                                            "sweep kernel, null when the kernel sources differ from the profiled",
                          "terms_samples_per_s": terms, "binding_term": binding,
                          "achieved_samples_per_s": samples_s, "frac_of_binding": samples_s / terms[binding],
