@@ -105,10 +105,16 @@ constexpr int kMaxBands = 1024;  // counters of the banded tile order (one per S
 // wide: the CTAs resident on an SM then overflow L1 with unrelated tiles'
 // footprints.  Measured, 8 sweeps: 3840x1920 FP16 textures 4-8 sources
 // 1-5 % faster, 2880x1440 FP16 6 sources 1 % faster, 3840x1920 u8 8 sources
-// 2 % faster; below 30 KB of source row bytes (1920x960 at any format and
-// count, 2400x1200 FP16, 3840x1920 u8 up to 6 sources) even or 1-4 % slower,
-// where L1 already holds the footprints (95 % hit rate at 1920x960 u8).
+// 2 % faster; below 30 KB of source row bytes at 1920x960 (any format and
+// count) even or 1-4 % slower, where L1 already holds the footprints (95 %
+// hit rate at 1920x960 u8).  From 2880 wide it pays from 21 KB with up to 7
+// sources (3 CTAs per SM): 3840x1920 u8 6 sources 2.6 % and 7 sources 0.8 %,
+// 2880x1440 FP16 4 sources 13 % and 5 sources 3.5 % faster; 2880x1440 u8
+// with 7 sources (20 KB) was even, and with 8 sources (2 CTAs per SM, 23 KB)
+// 1.4 % slower.
 constexpr size_t kBandedMinRowBytes = 30000;
+constexpr size_t kBandedMinRowBytesWide = 21000;  // W >= 2880, up to 7 sources
+constexpr int kBandedWideW = 2880;
 constexpr size_t kTexAlign = 512;
 
 int get_trig(pm_ctx *ctx, int W, int H, Trig *out) {
@@ -339,13 +345,15 @@ int ensure_textures(pm_request *r) {
 
 // Choose the tile order of a request: banded (persistent grid) for texture
 // sampling when the sources' row bytes W x bytes per texel x S reach
-// kBandedMinRowBytes, else one CTA per tile (the quad samplers measured
+// kBandedMinRowBytes (kBandedMinRowBytesWide from kBandedWideW pixels wide
+// with up to 7 sources), else one CTA per tile (the quad samplers measured
 // 4-6 % slower banded at 1920x960).
 void set_tile_order(pm_request *r) {
     r->banded_blocks = 0;
     if (r->ctx->n_sm <= 0 || r->ctx->n_sm > kMaxBands / 2 || r->prm.sampler != PM_SAMPLER_TEXTURE) return;
     const size_t texel = r->prm.image_format == PM_IMAGE_F16 ? 2 : 1;
-    if ((size_t)r->W * texel * (size_t)r->S < kBandedMinRowBytes) return;
+    const size_t min_row = (r->W >= kBandedWideW && r->S <= 7) ? kBandedMinRowBytesWide : kBandedMinRowBytes;
+    if ((size_t)r->W * texel * (size_t)r->S < min_row) return;
     const int bps = pm::dispatch_tile_blocks_per_sm(r->S, pm::image_kind(r->prm.image_format, r->prm.sampler));
     r->banded_blocks = bps > 0 ? bps * r->ctx->n_sm : 0;
 }
