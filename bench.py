@@ -65,6 +65,17 @@ FLOP_PER_SAMPLE = 40  # algorithmic FP32 work of one (pixel, hypothesis, source,
 SFU_PER_SAMPLE = 4    # special-function operations of one sample (rcp, rsqrt and the two angles)
 
 
+def _optional(fn, *a):
+    """One optional form's block, or {"error": ...} when it raises: the
+    headline line, measured before the optional forms, is printed either way."""
+    try:
+        return fn(*a)
+    except Exception as e:  # noqa: BLE001 - reported in the line, with its traceback on stderr
+        import traceback
+        traceback.print_exc()
+        return {"error": f"{type(e).__name__}: {e}"}
+
+
 def _mpix_views(ms: float) -> float:
     return (W * H / 1e6) * S / (ms / 1e3)
 
@@ -931,10 +942,10 @@ def run_ours(args):
     two_source = {"ms_per_sweep": min(two), "sources": 2, "W": W, "H": H,
                   "sweeps_value": (W * H / 1e6) * 2 / (SWEEPS * min(two) / 1e3), "unit": UNIT,
                   "note": "compare with reference_cuda in the --impl reference line (same scene and sizes)"}
-    served = None if args.no_served else run_served(native, scene, ctx, local, args)
-    batched = None if args.no_batched else run_batched(native, scene, ctx, local, args)
-    precision = None if args.no_precision else run_precision(native, scene, ctx, local)
-    pipeline = run_pipeline(native, scene, ctx, local, args.steps)
+    served = None if args.no_served else _optional(run_served, native, scene, ctx, local, args)
+    batched = None if args.no_batched else _optional(run_batched, native, scene, ctx, local, args)
+    precision = None if args.no_precision else _optional(run_precision, native, scene, ctx, local)
+    pipeline = _optional(run_pipeline, native, scene, ctx, local, args.steps)
     traffic = _traffic()
     # the roofline terms of the cost kernel (samples/s): 40 FP32 flop, 4
     # special-function operations and 1 bilinear fetch per sample
@@ -947,11 +958,13 @@ def run_ours(args):
     if rank == 0:
         cpu = None
         if not args.no_cpu and ws == 1:  # the CPU leg runs at N = 1 only
-            v, rows, secs, threads, _ = cpu_sample(target_s=args.cpu_seconds)
-            cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                   "sample": f"densification of {rows} rows x 1920 of the same workload (all {SWEEPS} sweeps, "
-                             f"top-3, reference float arithmetic, OpenMP) scaled to the keyframe, plus the "
-                             f"full-size consistency filter and fusion: {secs:.1f} s per keyframe"}
+            def cpu_leg():
+                v, rows, secs, threads, _ = cpu_sample(target_s=args.cpu_seconds)
+                return {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                        "sample": f"densification of {rows} rows x 1920 of the same workload (all {SWEEPS} "
+                                  f"sweeps, top-3, reference float arithmetic, OpenMP) scaled to the keyframe, "
+                                  f"plus the full-size consistency filter and fusion: {secs:.1f} s per keyframe"}
+            cpu = _optional(cpu_leg)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
