@@ -188,8 +188,8 @@ def _hbm_view(traffic, launch_ms):
 # (dram__bytes_read.sum + dram__bytes_write.sum), valid only for the kernel
 # sources it was measured on: a different build reports null rather than a
 # stale figure.
-TRAFFIC_NCU = {"bytes_per_launch": 59200256,
-               "sources_sha256": "9438004d4d43da521f24c31c08bde8f9f4b813a61cd9fb662c46bbb47b153174"}
+TRAFFIC_NCU = {"bytes_per_launch": 59333120,
+               "sources_sha256": "f912cb0b96066d4b68f0f251d91932f9acaad44aa0f2e23e1cf4dcf4387e1c02"}
 KERNEL_SOURCES = ("patchmatch_gb300/csrc/pm_sweep.cuh", "patchmatch_gb300/csrc/pm_device.cuh",
                   "patchmatch_gb300/csrc/pm_inst.cu", "patchmatch_gb300/csrc/pm_types.h")
 

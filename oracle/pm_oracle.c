@@ -446,6 +446,15 @@ static void init_pixel(const or_views *v, const or_run_params *rp, int i, int j,
     *depth = d;
 }
 
+/* A propagation neighbour outside the image is not a candidate.  Active
+ * pixels sit patch_half + 1 from every edge (PatchMatchCuda.cu:283), so this
+ * only matters for patch_half = 1, where the reference would read outside its
+ * buffers (it only ever runs patch_half = 5). */
+static int nbr_inside(const or_views *v, int ni, int nj)
+{
+    return ni >= 0 && ni < v->H && nj >= 0 && nj < v->W;
+}
+
 /* One pixel update of the reference's host variant (PatchMatchUpdatePixel,
  * depthmap.cc:1003-1067; CheckPlaneCandidate :1069-1078): pixels and
  * neighbours of depth 0 are ignored, candidates are compared by score alone
@@ -468,6 +477,7 @@ static void update_pixel_plain(const or_views *v, const or_run_params *rp, int s
     float b[3];
     run_bearing(v, &rp->cp, i, j, b);
     for (int a = 0; a < 8; ++a) {
+        if (!nbr_inside(v, i + adjacent[a][0], j + adjacent[a][1])) continue;
         size_t n = (size_t)(i + adjacent[a][0]) * W + (j + adjacent[a][1]);
         if (depthm[n] == 0.0f) continue;
         float pl[3] = {plane[3 * n], plane[3 * n + 1], plane[3 * n + 2]};
@@ -532,6 +542,7 @@ static void update_pixel(const or_views *v, const or_run_params *rp, int sweep, 
     run_bearing(v, &rp->cp, i, j, b);
     const float curr_depth = depthm[idx];
     for (int a = 0; a < 8; ++a) {
+        if (!nbr_inside(v, i + adjacent[a][0], j + adjacent[a][1])) continue;
         size_t n = (size_t)(i + adjacent[a][0]) * W + (j + adjacent[a][1]);
         float nx = plane[3 * n], ny = plane[3 * n + 1], nz = plane[3 * n + 2];
         float pl[3] = {nx, ny, nz};

@@ -240,6 +240,17 @@ __device__ __forceinline__ size_t nbr_index(int n, int i, int j, int W) {
     return (size_t)(i + di) * W + (j + dj);
 }
 
+// Whether propagation candidate n of pixel (i, j) lies inside the W x H image;
+// one outside is not a candidate.  Active pixels sit patch_half + 1 from every
+// edge (PatchMatchCuda.cu:283), so with patch_half >= 3 all eight are inside;
+// with patch_half = 1 the candidates 3 pixels out from the border pixels are not.
+__device__ __forceinline__ bool nbr_inside(int n, int i, int j, int W, int H) {
+    const int sel = n & 3, far = (n >> 2) ? 3 : 1;
+    const int di = (sel == 1) ? far : (sel == 3 ? -far : 0);
+    const int dj = (sel == 0) ? far : (sel == 2 ? -far : 0);
+    return (unsigned)(i + di) < (unsigned)H && (unsigned)(j + dj) < (unsigned)W;
+}
+
 // Window moments of plane (px, py, pz) at a pixel: the 36 taps x S sources of
 // the plane-induced warp (PatchMatchCuda.cu:100-157), one tap row and column
 // at a time from the staged tile.
@@ -433,7 +444,7 @@ __device__ __forceinline__ void tile_body(const A &a, int bx, int by, float4 *ti
             unsigned m = 0;
             if (active)
                 for (int n = from; n < kNbr; ++n) {
-                    if ((have >> n) & 1u) continue;
+                    if (((have >> n) & 1u) || !nbr_inside(n, i, j, W, H)) continue;
                     const float4 np = a.plane[nbr_index(n, i, j, W)];
                     const float f = smoothness_factor(np.x, np.y, np.z, hx, hy, hz, bxc, byc, bzc, curr_depth);
                     if (2.0f * f > score) m |= 1u << n;
@@ -464,6 +475,7 @@ __device__ __forceinline__ void tile_body(const A &a, int bx, int by, float4 *ti
                 // replay in order with the scores at hand (PatchMatchCuda.cu:305-337)
 #pragma unroll 1
                 for (; n < kNbr; ++n) {
+                    if (!nbr_inside(n, i, j, W, H)) continue;
                     const float4 np = a.plane[nbr_index(n, i, j, W)];
                     const float f = smoothness_factor(np.x, np.y, np.z, hx, hy, hz, bxc, byc, bzc, curr_depth);
                     if (!(2.0f * f > score)) continue;  // cannot be accepted (also when f is NaN)
@@ -500,6 +512,7 @@ __device__ __forceinline__ void tile_body(const A &a, int bx, int by, float4 *ti
             } else if (a.mode == kModeSeed) {
                 px = cand.x; py = cand.y; pz = cand.z;
             } else if (h < kNbr) {
+                if (!nbr_inside(h, i, j, W, H)) continue;
                 const float4 np = a.plane[nbr_index(h, i, j, W)];
                 px = np.x; py = np.y; pz = np.z;
                 if (plain) {

@@ -108,3 +108,35 @@ def test_cfg2_band_matches_oracle(ctx, sampler):
     assert a >= 0.99
     assert cg >= co - 0.01
     assert accg >= acco - 0.01
+
+
+def test_smallest_window_full_run_matches_oracle(ctx):
+    """patch_half = 1 (PatchSize 3): active pixels sit 2 from the border, so
+    the candidates 3 pixels out from the border pixels fall outside the image
+    and are not candidates, on the GPU and in the oracle alike.  A full run
+    (256x128, 4 sources, 8 sweeps, exact sampler) against the FP64 oracle at
+    the method's tolerance.  The raw agreement of the 3-pixel ring along the
+    border, where candidates fall outside, is printed: those pixels lie within
+    a few degrees of the poles and beside the longitude seam, where FP32 and
+    FP64 sample positions part most (the reason the other comparisons stay 6
+    pixels inside), so it sits below the interior's."""
+    req = scene.make_request(scene.ROOM, 256, 128, 4, seed=23)
+    r = _request(ctx, req, sampler=native.SAMPLER_EXACT, patch_half=1)
+    r.run()
+    g_raw, g_filt = r.read(raw=True), r.read()
+    r.close()
+    o = O.patchmatch(O.Views.from_request(req), O.cost_params(patch_half=1), iterations=SWEEPS)
+    o_filt = _oracle_filtered(req, o)
+    H, W = g_raw["depth"].shape
+    border = np.zeros((H, W), bool)
+    border[2:5, 2:W - 2] = border[H - 5:H - 1, 2:W - 2] = True
+    border[2:H - 2, 2:5] = border[2:H - 2, W - 5:W - 1] = True
+    assert (g_raw["depth"][border] > 0).all() and np.isfinite(g_raw["depth"][border]).all()
+    od = o["depth"][border]
+    ring = float((np.abs(g_raw["depth"][border] - od) < 0.01 * od).mean())
+    a, cg, co, araw, accg, acco = _agreement(g_raw["depth"], g_filt["depth"], o["depth"], o_filt, slice(None),
+                                             req.views[0].depth)
+    print(f"patch_half=1: valid-pixel agreement within 1% {a:.5f} (coverage gpu {cg:.4f} oracle {co:.4f}); "
+          f"raw interior agreement {araw:.5f}; raw agreement on the 3-pixel border ring {ring:.5f}")
+    assert a >= 0.99
+    assert cg >= co - 0.01

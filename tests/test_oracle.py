@@ -155,3 +155,13 @@ def test_host_cost_border_reads_zero(room):
     _, _, c = O.cost_batch(V, O.cost_params(seam=O.SEAM_CLAMP, combine=O.COMBINE_MAX), ij, planes, want_ncc=True)
     assert np.allclose(z[0], c[0], rtol=0, atol=1e-12)  # image centre: every sample inside
     assert np.abs(z[1:] - c[1:]).max() > 1e-3           # at the seam the border decides
+
+
+def test_smallest_window_skips_neighbours_outside_the_image():
+    """With patch_half = 1 the active region starts 2 pixels from the border;
+    the oracle's propagation skips the candidates that fall outside the image
+    (a full run touches every border pixel and stays finite)."""
+    req = scene.make_request(scene.ROOM, 64, 32, 2, seed=3)
+    o = O.patchmatch(O.Views.from_request(req), O.cost_params(patch_half=1), iterations=2)
+    d = o["depth"]
+    assert np.isfinite(d).all() and (d[2:30, 2:62] > 0).all()
