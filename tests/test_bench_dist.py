@@ -58,3 +58,13 @@ def test_reference_arm_under_torchrun_prints_once(built):
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["cpu_baseline"]["kind"] == "port"
+
+
+def test_failing_optional_form_is_reported_not_fatal():
+    """An optional form (served, batched, precision, pipeline, the CPU leg)
+    that raises becomes an error field of the line; the headline line is
+    still printed."""
+    sys.path.insert(0, ROOT)
+    import bench
+    assert bench._optional(lambda: {"value": 1.0}) == {"value": 1.0}
+    assert bench._optional(lambda x: 1 / x, 0) == {"error": "ZeroDivisionError: division by zero"}
